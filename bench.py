@@ -1,0 +1,395 @@
+"""Benchmark of the fused ERI + J/K build (the ERI GQuartet/s half of the metric).
+
+Workload: 64 H + 16 C/N/O atoms, seeded uniform positions in a 14 bohr cube
+(no pair closer than 1.3 bohr), 3-primitive contracted Cartesian s/p (H) and
+s/p/d (heavy) shells with exponents log-uniform in [0.1, 60] and coefficients
+uniform in [0.1, 1] -> 416 functions; one fused J and K build from a random
+symmetric PSD density; FP64; Schwarz threshold 1e-12 (Q_ab Q_cd max|D|).
+
+A step is one J/K build.  `value` is device-timed (CUDA events on the
+library's stream, density resident in HBM, L2 flushed before every step);
+`e2e` times the public C-ABI call qb_jk with pinned host buffers (density
+host->device and J, K device->host inside the timed region).  The unit of work
+is one canonical contracted shell quartet surviving the screening.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+METRIC = "ERI GQuartet/s (fused J+K build)"
+UNIT = "GQuartet/s"
+WORKLOAD = "ERI+J/K: 64 H + 16 C/N/O in a 14 bohr cube, 3-prim Cartesian s/p/d shells, N=416, FP64, Schwarz 1e-12"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--schwarz", type=float, default=1e-12)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,utilization.gpu,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        for line in Path(self.f.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        busy = [r for r in rows if r[2].isdigit() and int(r[2]) >= 50] or rows
+        sm = sorted(float(r[0]) for r in busy if r[0].replace(".", "").isdigit())
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[3 + k].lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None,
+                "sm_max_mhz": float(rows[0][1]) if rows[0][1].replace(".", "").isdigit() else None,
+                "reasons": reasons, "samples": len(rows), "samples_busy": len(busy)}
+
+
+# ---------------------------------------------------------------------------
+def workload(qb, seed):
+    from quiqbox_gb300.workloads import random_shell_molecule, random_density
+    atoms, coords, bs = random_shell_molecule(seed=seed)
+    fb = qb.flatten(bs)
+    return fb, random_density(fb.nfun, seed)
+
+
+def ncart(L):
+    return (L + 1) * (L + 2) // 2
+
+
+def survivors(pairs, dmax, thr):
+    """Per class (bra pair class, ket pair class): bra indices, per-bra counts, same-class flag."""
+    fa, fb_, la, lb, Q = pairs
+    pcs = sorted(set(zip(la.tolist(), lb.tolist())), key=lambda t: (t[0] * (t[0] + 1) // 2 + t[1]))
+    idx = {pc: np.where((la == pc[0]) & (lb == pc[1]))[0] for pc in pcs}
+    out = []
+    for x, X in enumerate(pcs):
+        for Y in pcs[:x + 1]:
+            bi, ki = idx[X], idx[Y]
+            qb_, qk = Q[bi], Q[ki]
+            if thr > 0:
+                t = np.where(qb_ > 0, thr / (dmax * np.where(qb_ > 0, qb_, 1.0)), np.inf)
+                cnt = np.searchsorted(-qk, -t, side="right")   # Q desc: number of Q_j >= t
+            else:
+                cnt = np.full(len(bi), len(ki))
+            same = X == Y
+            if same:
+                cnt = np.minimum(cnt, np.arange(len(bi)) + 1)
+            out.append({"cls": X + Y, "bra": bi, "ket": ki, "cnt": cnt.astype(np.int64), "same": same})
+    return out
+
+
+def expand(pairs, cls, picks):
+    """Shell quartets (i, j) of one class -> function quartets with degeneracy weights."""
+    fa, fb_, la, lb, Q = pairs
+    q, g = [], []
+    l1, l2, l3, l4 = cls["cls"]
+    for i, j in picks:
+        P, R = cls["bra"][i], cls["ket"][j]
+        deg = (1.0 if fa[P] == fb_[P] else 2.0) * (1.0 if fa[R] == fb_[R] else 2.0) * \
+              (1.0 if (cls["same"] and i == j) else 2.0)
+        for a in range(ncart(l1)):
+            for b in range(ncart(l2)):
+                for c in range(ncart(l3)):
+                    for d in range(ncart(l4)):
+                        q.append((fa[P] + a, fb_[P] + b, fa[R] + c, fb_[R] + d))
+                        g.append(deg)
+    return np.asarray(q, np.int32).reshape(-1, 4), np.asarray(g)
+
+
+def cpu_baseline(oracle, fb, D, pairs, thr, budget_s, seed=0):
+    """Oracle (CPU port of the reference's per-primitive algorithm) on a stratified
+    random sample of the surviving shell quartets, all host threads.  Returns the
+    estimated full-workload rate and the details."""
+    rng = np.random.default_rng(seed)
+    dmax = float(np.abs(D).max())
+    classes = survivors(pairs, dmax, thr)
+    nthreads = oracle.num_threads()
+    total_q, est_time, sampled, spent = 0, 0.0, 0, 0.0
+    # calibration: a small batch per class
+    cost = {}
+    for cl in classes:
+        n = int(cl["cnt"].sum())
+        cl["n"] = n
+        total_q += n
+        if n == 0:
+            continue
+        offs = np.concatenate([[0], np.cumsum(cl["cnt"])])
+        cl["offs"] = offs
+        m = min(n, max(2, nthreads))
+        t = rng.integers(0, n, m)
+        i = np.searchsorted(offs, t, side="right") - 1
+        picks = list(zip(i.tolist(), (t - offs[i]).tolist()))
+        q, g = expand(pairs, cl, picks)
+        t0 = time.perf_counter()
+        oracle.jk_list(fb, q, g, D, nthreads)
+        dt = time.perf_counter() - t0
+        cost[id(cl)] = (dt, m)
+        spent += dt
+        sampled += m
+    # main passes: the remaining budget spread by each class's share of the estimated time
+    live = [cl for cl in classes if cl["n"]]
+    for _ in range(3):
+        remaining = budget_s - spent
+        if remaining <= 0.05 * budget_s:
+            break
+        share = {id(cl): cl["n"] * cost[id(cl)][0] / cost[id(cl)][1] for cl in live}
+        tot = sum(share.values()) or 1.0
+        for cl in live:
+            dt0, m0 = cost[id(cl)]
+            per = dt0 / m0
+            m = int(min(cl["n"], (remaining * share[id(cl)] / tot) / max(per, 1e-9)))
+            if m < nthreads:
+                continue
+            t = rng.integers(0, cl["n"], m)
+            offs = cl["offs"]
+            i = np.searchsorted(offs, t, side="right") - 1
+            picks = list(zip(i.tolist(), (t - offs[i]).tolist()))
+            q, g = expand(pairs, cl, picks)
+            t0 = time.perf_counter()
+            oracle.jk_list(fb, q, g, D, nthreads)
+            dt = time.perf_counter() - t0
+            spent += dt
+            sampled += m
+            cost[id(cl)] = (dt0 + dt, m0 + m)
+    for cl in live:
+        dt0, m0 = cost[id(cl)]
+        est_time += cl["n"] * dt0 / m0
+    rate = total_q / est_time / 1e9
+    return {"value": rate, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{sampled} of {total_q} surviving shell quartets, stratified by class; "
+                      f"{spent:.1f} s of CPU work; full build estimated at {est_time:.1f} s",
+            "est_build_s": est_time, "quartets": total_q}
+
+
+def oracle_pairs(oracle, qb, fb):
+    """Shell-pair table with Schwarz factors computed by the oracle (CPU only)."""
+    from quiqbox_gb300.basis import FlatBasis
+    fp = fb.fun_ptr
+    shells = []   # (first function, L)
+    f = 0
+    while f < fb.nfun:
+        L = int(fb.ijk[fp[f]].sum())
+        shells.append((f, L))
+        f += ncart(L)
+    rows = []
+    for a in range(len(shells)):
+        for b in range(a + 1):
+            A, B = shells[a], shells[b]
+            if B[1] > A[1]:
+                A, B = B, A
+            rows.append((A[0], B[0], A[1], B[1]))
+    quart = []
+    for (x, y, l1, l2) in rows:
+        for i in range(ncart(l1)):
+            for j in range(ncart(l2)):
+                quart.append((x + i, y + j, x + i, y + j))
+    vals = oracle.eri_list(fb, np.asarray(quart, np.int32))
+    k = 0
+    fa, fbb, la, lb, Q = [], [], [], [], []
+    for (x, y, l1, l2) in rows:
+        m = ncart(l1) * ncart(l2)
+        Q.append(np.sqrt(np.abs(vals[k:k + m]).max()))
+        k += m
+        fa.append(x); fbb.append(y); la.append(l1); lb.append(l2)
+    fa, fbb, la, lb, Q = map(np.asarray, (fa, fbb, la, lb, Q))
+    order = np.lexsort((-Q, lb, la))
+    return fa[order], fbb[order], la[order], lb[order], Q[order]
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
+    import __graft_entry__ as ge
+    import oracle
+    qb = ge.load_package()
+    oracle.lib()
+    fb, D = workload(qb, args.seed)
+    pairs = oracle_pairs(oracle, qb, fb)
+    per_step = max(3.0, args.cpu_seconds / 2)
+    for _ in range(args.warmup):
+        cpu_baseline(oracle, fb, D, pairs, args.schwarz, 0.5, seed=99)
+    vals, ests, last = [], [], None
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        last = cpu_baseline(oracle, fb, D, pairs, args.schwarz, per_step, seed=s)
+        vals.append(last["value"])
+        ests.append(last["est_build_s"])
+    wall = time.perf_counter() - t0
+    value = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(ests)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generator; no dataset)",
+            "config": {"workload": WORKLOAD, "nfun": fb.nfun, "schwarz": args.schwarz,
+                       "quartets": last["quartets"], "parallelism": "host threads (OpenMP)",
+                       "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": last["cores"], "kind": "port",
+                             "sample": last["sample"] + f"; {args.steps} sampled steps in {wall:.1f} s wall"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    rank, local_rank, world = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    import torch
+    import __graft_entry__ as ge
+    qb = ge.load_package()
+    from quiqbox_gb300 import _lib as L
+    ctx = qb.Context(local_rank)
+    lib = ctx.lib
+    fb, D = workload(qb, args.seed)
+    n = fb.nfun
+    b = L.BasisArgs(fb)
+    ctx.check(lib.qb_jk_prepare(ctx.h, b.ref(), args.schwarz))
+    # pinned host buffers
+    Dp = torch.empty(n * n, dtype=torch.float64, pin_memory=True).numpy()
+    Dp[:] = D.reshape(-1, order="F")
+    Jp = torch.empty(n * n, dtype=torch.float64, pin_memory=True).numpy()
+    Kp = torch.empty(n * n, dtype=torch.float64, pin_memory=True).numpy()
+    ctx.check(lib.qb_jk_upload_density(ctx.h, L.dptr(Dp)))
+    stats = L.QBJKStats()
+    for _ in range(args.warmup):
+        ctx.check(lib.qb_jk_execute(ctx.h))
+        ctx.check(lib.qb_jk_get_stats(ctx.h, C.byref(stats)))
+    peak = qb.fp64_peak(ctx)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
+    launches_per_step = 3 + sum(1 for c in range(stats.nclass) if stats.class_quartets[c] > 0)
+    clocks = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ms, flops, quartets = [], [], []
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ctx.check(lib.qb_jk_execute(ctx.h))
+        ctx.check(lib.qb_jk_get_stats(ctx.h, C.byref(stats)))
+        ms.append(stats.ms_last)
+        flops.append(stats.flops)
+        quartets.append(stats.quartets)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    total_ms = float(np.sum(ms))
+    q = int(quartets[-1])
+    # e2e through the public call with host buffers
+    e2e_s = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        ctx.check(lib.qb_jk(ctx.h, b.ref(), L.dptr(Dp), args.schwarz, L.dptr(Jp), L.dptr(Kp)))
+        e2e_s.append(time.perf_counter() - t0)
+    if dist:
+        t = torch.tensor([total_ms, float(np.sum(e2e_s))], dtype=torch.float64, device=f"cuda:{local_rank}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, e2e_tot = float(t[0]), float(t[1])
+    else:
+        e2e_tot = float(np.sum(e2e_s))
+    value = world * q * args.steps / (total_ms * 1e-3) / 1e9
+    e2e_value = world * q * args.steps / e2e_tot / 1e9
+    achieved = float(np.mean(flops)) / (total_ms / args.steps * 1e-3) / 1e12
+    J = Jp.reshape((n, n), order="F")
+    K = Kp.reshape((n, n), order="F")
+    sym = float(max(np.abs(J - J.T).max() / np.abs(J).max(), np.abs(K - K.T).max() / np.abs(K).max()))
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generator; no dataset)",
+            "config": {"workload": WORKLOAD, "nfun": n, "nshell": stats.nshell, "npair": stats.npair,
+                       "schwarz": args.schwarz, "quartets": q, "prim_quartets": int(stats.prim_quartets),
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "l2": "flushed (256 MiB write) before every timed step",
+                       "wall_s_timed_region": wall, "jk_symmetry_rel": sym},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "peak_source": "measured: FP64 FMA microbenchmark (qb_fp64_peak) in this run",
+                         "flops_per_step": float(np.mean(flops)),
+                         "flops_source": "per-class FP64 op counts of the generated kernels x quartets"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * n * 8,
+                    "d2h_bytes_per_step": 2 * n * n * 8, "ms_per_step": 1e3 * e2e_tot / args.steps},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clk}
+    if world == 1:
+        import oracle
+        oracle.lib()
+        arr = [np.zeros(stats.npair, np.int32) for _ in range(4)]
+        Qv = np.zeros(stats.npair)
+        npair = C.c_int()
+        ctx.check(lib.qb_jk_pair_table(ctx.h, C.byref(npair), *[L.iptr(a) for a in arr], L.dptr(Qv)))
+        pairs = (arr[0], arr[1], arr[2], arr[3], Qv)
+        line["cpu_baseline"] = cpu_baseline(oracle, fb, D, pairs, args.schwarz, args.cpu_seconds)
+        line["cpu_baseline"].pop("quartets", None)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.warmup < 3:
+        a.warmup = 3
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

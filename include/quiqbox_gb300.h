@@ -1,0 +1,156 @@
+/* quiqbox_gb300.h — C ABI of the GB300 (sm_103a) integral and Hartree–Fock path.
+ *
+ * Drop-in native back end for Quiqbox.jl's Gaussian-orbital integral API and
+ * its RHF/UHF driver.  Plain C types only: the Julia side (basis containers,
+ * parameter graph, SCF configuration) stays in Julia and binds these symbols
+ * with `ccall`.  All matrices are column-major (Julia's layout).
+ *
+ * Conventions
+ *  - A basis is `nfun` contracted functions; function f owns the primitives
+ *    fun_ptr[f] .. fun_ptr[f+1]-1.  Every primitive has its own centre, Cartesian
+ *    powers (i,j,k), exponent and *effective* weight: the contraction coefficient
+ *    with every normalisation factor already applied, exactly the weights that
+ *    `getOrbCorePointers` / `buildOrbCoreWeight!` produce
+ *    (src/Integration/Framework.jl:748-825).
+ *  - Outputs are caller-allocated host arrays; the library owns all device memory
+ *    and keeps no pointer to caller memory after a call returns.
+ *  - Every entry point returns a status (QB_OK or QB_ERR_*) and never aborts;
+ *    qb_last_error() gives the message.  One context must not be used by two
+ *    threads at once.
+ */
+#ifndef QUIQBOX_GB300_H
+#define QUIQBOX_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    QB_OK = 0,
+    QB_ERR_ARG = 1,            /* bad pointer / argument  (AssertionError, src/Exception.jl)          */
+    QB_ERR_DIM = 2,            /* size mismatch           (DimensionMismatch, src/HartreeFock.jl:200) */
+    QB_ERR_DOMAIN = 3,         /* out-of-domain value     (DomainError, src/HartreeFock.jl:989,994)   */
+    QB_ERR_CUDA = 4,           /* CUDA runtime failure                                                */
+    QB_ERR_TIMEOUT = 5,        /* a bounded device wait ran out                                       */
+    QB_ERR_NOT_CONVERGED = 6,  /* SCF stopped without convergence (converged = false, :800)           */
+    QB_ERR_NOMEM = 7,          /* device allocation failed                                            */
+    QB_ERR_UNSUPPORTED = 8     /* angular momentum beyond the kernels' limits                         */
+};
+
+typedef struct qb_ctx qb_ctx;
+
+typedef struct {
+    int nfun;
+    const int* fun_ptr;     /* nfun + 1                   */
+    const double* center;   /* 3 * nprim, (x, y, z) each  */
+    const int* ijk;         /* 3 * nprim                  */
+    const double* alpha;    /* nprim                      */
+    const double* weight;   /* nprim, effective weights   */
+} qb_basis;
+
+/* Context: one per host thread; owns device buffers, streams and the Boys table. */
+int qb_create(qb_ctx** out, int device);
+void qb_destroy(qb_ctx* ctx);
+const char* qb_last_error(const qb_ctx* ctx);
+int qb_device_info(qb_ctx* ctx, int* sm_count, int* cc_major, int* cc_minor);
+
+/* One-electron matrices, nfun x nfun.
+ * overlaps        <- src/Integration/Interface.jl:46  (overlaps)
+ * elecKinetics    <- src/Integration/Interface.jl:143 (elecKinetics)
+ * nucAttractions  <- src/Integration/Interface.jl:236 (nucAttractions; V = -sum_C Z_C (a|1/r_C|b))
+ * coreHamiltonian <- src/Integration/Interface.jl:288 (coreHamiltonian = kinetic + nuclear) */
+int qb_overlaps(qb_ctx* ctx, const qb_basis* basis, double* S);
+int qb_elec_kinetics(qb_ctx* ctx, const qb_basis* basis, double* T);
+int qb_nuc_attractions(qb_ctx* ctx, const qb_basis* basis, int nnuc, const double* Z, const double* R,
+                       double* V);
+int qb_core_hamiltonian(qb_ctx* ctx, const qb_basis* basis, int nnuc, const double* Z, const double* R,
+                        double* H);
+
+/* Two-electron integrals (chemists' notation (ij|kl)).
+ * qb_elec_repulsions <- src/Integration/Interface.jl:356 (elecRepulsions): nfun^4 tensor [i,j,k,l]
+ * qb_elec_repulsion_list <- src/Integration/Interface.jl:331 (elecRepulsion) for nq explicit
+ *                           0-based quartets (4 ints each) */
+int qb_elec_repulsions(qb_ctx* ctx, const qb_basis* basis, double* eri);
+int qb_elec_repulsion_list(qb_ctx* ctx, const qb_basis* basis, int64_t nq, const int* quartets,
+                           double* out);
+
+/* Direct Coulomb and exchange matrices of a symmetric density D, no stored ERIs:
+ *   J_ij = sum_kl (ij|kl) D_kl,   K_ij = sum_kl (ik|jl) D_kl.
+ * Replaces the stored-tensor contraction of getGcore (src/HartreeFock.jl:305-319):
+ * G = 2J(D) - K(D) for RHF, G^s = J(Da+Db) - K(D^s) for UHF.
+ * Shell quartets with Q_ab Q_cd max|D| < schwarz are skipped (Q = Schwarz factors). */
+int qb_jk(qb_ctx* ctx, const qb_basis* basis, const double* D, double schwarz, double* J, double* K);
+
+/* Split form of qb_jk for callers that keep the density on the device between
+ * builds (and for timing): prepare the basis once, then upload / execute / download. */
+int qb_jk_prepare(qb_ctx* ctx, const qb_basis* basis, double schwarz);
+int qb_jk_upload_density(qb_ctx* ctx, const double* D);
+int qb_jk_execute(qb_ctx* ctx);
+int qb_jk_download(qb_ctx* ctx, double* J, double* K);
+
+typedef struct {
+    int shell_path;               /* 1: generated shell-class kernels, 0: generic per-function kernels */
+    int nshell, npair, nclass;
+    int64_t quartets;             /* canonical shell quartets surviving the screening (last execute)  */
+    int64_t prim_quartets;        /* primitive quartets evaluated (last execute)                      */
+    double flops;                 /* FP64 flops of the last execute (generated-code op counts)        */
+    double ms_last;               /* device time of the last execute (CUDA events)                    */
+    int64_t class_quartets[32];
+    int64_t class_prim_quartets[32];
+    int class_l[32][4];
+} qb_jk_stats;
+int qb_jk_get_stats(qb_ctx* ctx, qb_jk_stats* stats);
+
+/* Introspection (no reference counterpart): the shell-pair table of the prepared
+ * basis in the order the J/K kernels use it, grouped by pair class (la, lb) and
+ * sorted by descending Schwarz factor within a class.  Pass null arrays to get
+ * *npair only; otherwise each array holds *npair entries.  fa / fb are the first
+ * function indices of the two shells (A is the shell of higher angular momentum). */
+int qb_jk_pair_table(qb_ctx* ctx, int* npair, int* fa, int* fb, int* la, int* lb, double* Q);
+
+/* Hartree–Fock SCF (runHartreeFock, src/HartreeFock.jl:953-1228) on the GPU:
+ * symmetric orthogonalisation, Jacobi diagonalisation, direct J/K Fock build,
+ * DD / DIIS / EDIIS / ADIIS convergence methods (Lagrange-multiplier solver). */
+enum { QB_SCF_DD = 0, QB_SCF_DIIS = 1, QB_SCF_EDIIS = 2, QB_SCF_ADIIS = 3 };
+enum { QB_GUESS_COREH = 0, QB_GUESS_GWH = 1, QB_GUESS_SAD = 2, QB_GUESS_DIRECT = 3 };
+
+typedef struct {
+    int uhf;                      /* 0 RHF (n_alpha == n_beta required), 1 UHF                   */
+    int guess;                    /* QB_GUESS_*                                                  */
+    const double* C0;             /* QB_GUESS_DIRECT: (1 or 2) nfun x nfun coefficient matrices */
+    int nmethod;                  /* 1..8                                                        */
+    int method[8];                /* QB_SCF_*                                                    */
+    double interval[8];           /* per-method stopping thresholds; the last converges          */
+    double secondary_ratio[2];    /* RMS(FDS-SDF) and RMS(dD) ratios (default 1000, 1000)        */
+    double oscillate_threshold;   /* default 5e-6                                                */
+    int max_step;                 /* default 200                                                 */
+    int early_stop;               /* default 1                                                   */
+    int diis_size;                /* default 15                                                  */
+    double damp_strength;         /* DD damping, default 0.75                                    */
+    double schwarz;               /* J/K screening threshold (default 1e-14)                     */
+} qb_scf_config;
+
+typedef struct {
+    double E_elec;                /* electronic energy (Ha)                                      */
+    double E_nuc;                 /* nuclear repulsion (Ha)                                      */
+    int converged;                /* 0 no, 1 yes, 2 converged to an oscillation                  */
+    int steps;
+    double dE, rms_dD, rms_FDS;   /* last-step convergence indicators                            */
+    double* C;                    /* optional outputs (caller-allocated, nspin * nfun^2 / nfun)  */
+    double* D;
+    double* F;
+    double* eps;
+} qb_scf_result;
+
+void qb_scf_config_default(qb_scf_config* cfg);
+int qb_run_hartree_fock(qb_ctx* ctx, const qb_basis* basis, int nnuc, const double* Z, const double* R,
+                        int n_alpha, int n_beta, const qb_scf_config* cfg, qb_scf_result* res);
+
+/* Measured FP64 FMA throughput of this device (TFLOP/s), the FP64 roofline denominator. */
+int qb_fp64_peak(qb_ctx* ctx, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QUIQBOX_GB300_H */

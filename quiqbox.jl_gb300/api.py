@@ -1,0 +1,299 @@
+"""Host-side mirror of Quiqbox.jl's exported integral API and its Hartree–Fock
+entry point, each calling the GB300 C ABI.
+
+Names, argument meaning and error behaviour follow the reference:
+``overlap(s)``, ``elecKinetic(s)``, ``nucAttraction(s)``, ``coreHamiltonian``,
+``elecRepulsion(s)`` (src/Integration/Interface.jl:21-365) and
+``runHartreeFock`` with ``HFconfig`` / ``SCFconfig`` (src/HartreeFock.jl:659-1046).
+Matrices come back as numpy arrays in the reference's index order.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+from .basis import (CompositeOrb, FlatBasis, NuclearCluster, PrimitiveOrb, flatten, nucRepulsion,
+                    prepareSpinConfiguration, NUCLEAR_CHARGE)
+
+DimensionMismatch = L.DimensionMismatch
+DomainError = L.DomainError
+
+
+def _ctx(ctx):
+    return ctx if ctx is not None else L.default_context()
+
+
+def _flat(basis) -> FlatBasis:
+    if isinstance(basis, FlatBasis):
+        return basis
+    if isinstance(basis, (PrimitiveOrb, CompositeOrb)):
+        basis = [basis]
+    basis = list(basis)
+    if not basis:
+        raise ValueError("AssertionError: the basis set must not be empty")
+    return flatten(basis)
+
+
+def _nuclei(nucs, coords=None):
+    """(charges, positions) from a NuclearCluster or from symbol / coordinate lists."""
+    if isinstance(nucs, NuclearCluster):
+        return nucs.charges, nucs.positions
+    if coords is None or len(nucs) != len(coords):
+        raise ValueError("AssertionError: `nucs` and `coords` should have the same length.")
+    Z = np.array([NUCLEAR_CHARGE[s] if isinstance(s, str) else float(s) for s in nucs], np.float64)
+    return Z, np.asarray(coords, np.float64).reshape(-1, 3)
+
+
+def _matrix(fn, fb, ctx, *extra):
+    c = _ctx(ctx)
+    b = L.BasisArgs(fb)
+    out = np.zeros(fb.nfun * fb.nfun)
+    c.check(fn(c.h, b.ref(), *extra, L.dptr(out)))
+    return out.reshape((fb.nfun, fb.nfun), order="F")
+
+
+def overlaps(basis, ctx=None):
+    """S_ij = <i|j> (Interface.jl:46)."""
+    fb = _flat(basis)
+    return _matrix(_ctx(ctx).lib.qb_overlaps, fb, ctx)
+
+
+def overlap(b1, b2, ctx=None):
+    """<b1|b2> (Interface.jl:21)."""
+    return overlaps([b1, b2], ctx)[0, 1]
+
+
+def elecKinetics(basis, ctx=None):
+    """T_ij = <i|-1/2 ∇²|j> (Interface.jl:143)."""
+    return _matrix(_ctx(ctx).lib.qb_elec_kinetics, _flat(basis), ctx)
+
+
+def elecKinetic(b1, b2, ctx=None):
+    return elecKinetics([b1, b2], ctx)[0, 1]
+
+
+def _with_nuclei(fn, basis, nucs, coords, ctx):
+    fb = _flat(basis)
+    Z, R = _nuclei(nucs, coords)
+    Zc = np.ascontiguousarray(Z)
+    Rc = np.ascontiguousarray(R.reshape(-1))
+    return _matrix(fn, fb, ctx, len(Zc), L.dptr(Zc), L.dptr(Rc))
+
+
+def nucAttractions(nucs, coords_or_basis, basis=None, ctx=None):
+    """V_ij = -Σ_C Z_C <i|1/|r-R_C||j> (Interface.jl:186-256).
+
+    nucAttractions(nucs, coords, basis) or nucAttractions(nuclearCluster, basis)."""
+    if isinstance(nucs, NuclearCluster):
+        return _with_nuclei(_ctx(ctx).lib.qb_nuc_attractions, coords_or_basis, nucs, None, ctx)
+    return _with_nuclei(_ctx(ctx).lib.qb_nuc_attractions, basis, nucs, coords_or_basis, ctx)
+
+
+def nucAttraction(nucs, coords, b1, b2=None, ctx=None):
+    if isinstance(nucs, NuclearCluster):
+        return nucAttractions(nucs, [coords, b1], ctx=ctx)[0, 1]
+    return nucAttractions(nucs, coords, [b1, b2], ctx=ctx)[0, 1]
+
+
+def coreHamiltonian(nucs, coords_or_basis, basis=None, ctx=None):
+    """H = T + V (Interface.jl:288-312)."""
+    if isinstance(nucs, NuclearCluster):
+        return _with_nuclei(_ctx(ctx).lib.qb_core_hamiltonian, coords_or_basis, nucs, None, ctx)
+    return _with_nuclei(_ctx(ctx).lib.qb_core_hamiltonian, basis, nucs, coords_or_basis, ctx)
+
+
+def elecRepulsions(basis, ctx=None):
+    """Full (ij|kl) tensor, index order [i, j, k, l] (Interface.jl:356-365)."""
+    fb = _flat(basis)
+    n = fb.nfun
+    c = _ctx(ctx)
+    b = L.BasisArgs(fb)
+    out = np.zeros(n ** 4)
+    c.check(c.lib.qb_elec_repulsions(c.h, b.ref(), L.dptr(out)))
+    return out.reshape((n, n, n, n), order="F")
+
+
+def elecRepulsion_list(basis, quartets, ctx=None):
+    """(ij|kl) for explicit 0-based quartets."""
+    fb = _flat(basis)
+    q = np.ascontiguousarray(np.asarray(quartets, np.int32).reshape(-1, 4))
+    c = _ctx(ctx)
+    b = L.BasisArgs(fb)
+    out = np.zeros(len(q))
+    c.check(c.lib.qb_elec_repulsion_list(c.h, b.ref(), len(q), L.iptr(q), L.dptr(out)))
+    return out
+
+
+def elecRepulsion(b1, b2, b3, b4, ctx=None):
+    """(b1 b2|b3 b4) (Interface.jl:331)."""
+    return float(elecRepulsion_list([b1, b2, b3, b4], [(0, 1, 2, 3)], ctx)[0])
+
+
+def jk(basis, D, schwarz=1e-12, ctx=None):
+    """Direct J_ij = Σ (ij|kl) D_kl and K_ij = Σ (ik|jl) D_kl without a stored ERI tensor."""
+    fb = _flat(basis)
+    n = fb.nfun
+    Dm = np.asarray(D, np.float64)
+    if Dm.shape != (n, n):
+        raise DimensionMismatch(f"density is {Dm.shape}, basis has {n} functions")
+    Df = np.ascontiguousarray(Dm.reshape(-1, order="F"))
+    J = np.zeros(n * n)
+    K = np.zeros(n * n)
+    c = _ctx(ctx)
+    b = L.BasisArgs(fb)
+    c.check(c.lib.qb_jk(c.h, b.ref(), L.dptr(Df), float(schwarz), L.dptr(J), L.dptr(K)))
+    return J.reshape((n, n), order="F"), K.reshape((n, n), order="F")
+
+
+# ---------------------------------------------------------------------------
+RCHartreeFock = "RHF"   # restricted closed-shell (HartreeFock.jl:61)
+UOHartreeFock = "UHF"   # unrestricted open-shell (HartreeFock.jl:62)
+_METHODS = {"DD": 0, "DIIS": 1, "EDIIS": 2, "ADIIS": 3}
+_GUESSES = {"CoreH": 0, "GWH": 1, "SAD": 2, "Direct": 3}
+
+
+@dataclass
+class SCFconfig:
+    """SCF strategy (HartreeFock.jl:659-693): methods with their stopping thresholds
+    (the last converges), per-method keywords (DIISsize, dampStrength; the DIIS
+    coefficient problem uses the Lagrange-multiplier solver), secondary
+    convergence ratios and the oscillation threshold."""
+    methods: Sequence[str] = ("DD", "ADIIS", "DIIS")
+    intervals: Sequence[float] = (5e-3, 1e-4, 1e-9)
+    config: dict = field(default_factory=dict)
+    secondaryConvRatio: Sequence[float] = (1000.0, 1000.0)
+    oscillateThreshold: float = 5e-6
+
+    def __post_init__(self):
+        if len(self.methods) != len(self.intervals) or not self.methods:
+            raise ValueError("AssertionError: methods and intervals must have the same non-zero length")
+        for m in self.methods:
+            if m not in _METHODS:
+                raise ValueError(f"unknown SCF method {m}")
+        if np.ndim(self.secondaryConvRatio) == 0:
+            self.secondaryConvRatio = (float(self.secondaryConvRatio),) * 2
+
+    @classmethod
+    def default(cls, threshold=1e-9, secondaryConvRatio=(1000.0, 1000.0), oscillateThreshold=5e-6):
+        """SCFconfig(; threshold) (HartreeFock.jl:695-701)."""
+        return cls(("DD", "ADIIS", "DIIS"), (5e-3, 1e-4, float(threshold)), {}, secondaryConvRatio,
+                   oscillateThreshold)
+
+
+@dataclass
+class HFconfig:
+    """Hartree–Fock configuration (HartreeFock.jl:874-904)."""
+    type: str = RCHartreeFock
+    initial: object = "SAD"       # "CoreH" | "GWH" | "SAD" | tuple of coefficient matrices (Direct)
+    strategy: SCFconfig = field(default_factory=SCFconfig)
+    maxStep: int = 200
+    earlyStop: bool = True
+    schwarz: float = 1e-14
+
+    def __post_init__(self):
+        if self.maxStep < 1:
+            raise DomainError("maxStep must be positive")
+
+
+@dataclass
+class HFfinalInfo:
+    """Final values of an SCF run (HartreeFock.jl:791-819)."""
+    energy: tuple                 # (E_elec, E_nuc)
+    coeff: tuple
+    density: tuple
+    fock: tuple
+    occu: tuple                   # per sector: (orbital energies, occupations)
+    converged: object
+    steps: int
+    spin: tuple
+
+
+def runHartreeFock(nucInfo, basis, config: Optional[HFconfig] = None, spin=None, ctx=None) -> HFfinalInfo:
+    """runHartreeFock (HartreeFock.jl:953-1046) on the GPU.
+
+    nucInfo: NuclearCluster; spin: (nAlpha, nBeta) or None for the neutral,
+    maximally paired configuration (prepareSpinConfiguration, src/Particles.jl:146-170)."""
+    if not isinstance(nucInfo, NuclearCluster):
+        raise ValueError("nucInfo must be a NuclearCluster")
+    fb = _flat(basis)
+    n = fb.nfun
+    na, nb = spin if spin is not None else prepareSpinConfiguration(nucInfo)
+    if config is None:
+        config = HFconfig(type=RCHartreeFock if (na + nb) % 2 == 0 else UOHartreeFock)
+    uhf = config.type == UOHartreeFock
+    if not uhf and na != nb:
+        raise ValueError("AssertionError: Close-shell system must have the same number of spins for both "
+                         "spin orientations.")
+    nsec = 2 if uhf else 1
+    cfg = L.QBSCFConfig()
+    c = _ctx(ctx)
+    c.lib.qb_scf_config_default(C.byref(cfg))
+    cfg.uhf = int(uhf)
+    C0 = None
+    if isinstance(config.initial, str):
+        cfg.guess = _GUESSES[config.initial]
+    else:
+        mats = list(config.initial)
+        if len(mats) != nsec or any(np.asarray(m).shape != (n, n) for m in mats):
+            raise DimensionMismatch("The size/sizes of the input initial orbital coefficient matrix/matrices "
+                                    f"does not match the basis-set size ({n}).")
+        C0 = np.ascontiguousarray(np.concatenate([np.asarray(m, np.float64).reshape(-1, order="F") for m in mats]))
+        cfg.guess = 3
+        cfg.C0 = L.dptr(C0)
+    st = config.strategy
+    cfg.nmethod = len(st.methods)
+    for k, (m, iv) in enumerate(zip(st.methods, st.intervals)):
+        cfg.method[k] = _METHODS[m]
+        cfg.interval[k] = float(iv)
+    kw = {}
+    for d in st.config.values():
+        kw.update(dict(d))
+    cfg.diis_size = int(kw.get("DIISsize", 15))
+    cfg.damp_strength = float(kw.get("dampStrength", 0.75))
+    cfg.secondary_ratio[0] = float(st.secondaryConvRatio[0])
+    cfg.secondary_ratio[1] = float(st.secondaryConvRatio[1])
+    cfg.oscillate_threshold = float(st.oscillateThreshold)
+    cfg.max_step = int(config.maxStep)
+    cfg.early_stop = int(bool(config.earlyStop))
+    cfg.schwarz = float(config.schwarz)
+    Cb, Db, Fb = (np.zeros(nsec * n * n) for _ in range(3))
+    eps = np.zeros(nsec * n)
+    res = L.QBSCFResult()
+    res.C, res.D, res.F, res.eps = L.dptr(Cb), L.dptr(Db), L.dptr(Fb), L.dptr(eps)
+    Z = np.ascontiguousarray(nucInfo.charges)
+    R = np.ascontiguousarray(nucInfo.positions.reshape(-1))
+    b = L.BasisArgs(fb)
+    c.check(c.lib.qb_run_hartree_fock(c.h, b.ref(), len(Z), L.dptr(Z), L.dptr(R), int(na), int(nb),
+                                      C.byref(cfg), C.byref(res)), allow=(L.QB_ERR_NOT_CONVERGED,))
+    mats = lambda buf: tuple(buf[k * n * n:(k + 1) * n * n].reshape((n, n), order="F") for k in range(nsec))
+    occ = []
+    for k in range(nsec):
+        e = eps[k * n:(k + 1) * n]
+        if uhf:
+            nk = (na, nb)[k]
+            mark = (True, False) if k == 0 else (False, True)
+            occ.append((e, [mark if i < nk else (False, False) for i in range(n)]))
+        else:
+            occ.append((e, [(True, True) if 2 * (i + 1) <= na + nb else (False, False) for i in range(n)]))
+    conv = {0: False, 1: True, 2: True}[res.converged]
+    return HFfinalInfo((res.E_elec, nucRepulsion(nucInfo)), mats(Cb), mats(Db), mats(Fb), tuple(occ), conv,
+                       res.steps, (na, nb))
+
+
+def fp64_peak(ctx=None):
+    """Measured FP64 FMA throughput of the device (TFLOP/s)."""
+    c = _ctx(ctx)
+    out = C.c_double()
+    c.check(c.lib.qb_fp64_peak(c.h, C.byref(out)))
+    return out.value
+
+
+def device_info(ctx=None):
+    c = _ctx(ctx)
+    sm, ma, mi = C.c_int(), C.c_int(), C.c_int()
+    c.check(c.lib.qb_device_info(c.h, C.byref(sm), C.byref(ma), C.byref(mi)))
+    return {"sm_count": sm.value, "cc": (ma.value, mi.value)}

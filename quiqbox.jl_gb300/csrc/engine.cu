@@ -1,0 +1,516 @@
+// Integral engine: basis upload, shell detection, shell pairs, Schwarz screening,
+// class work lists and the fused ERI + J/K build.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+#include "qb_internal.h"
+
+int qb_set_error(qb_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+int qb_cuda_check(qb_ctx* ctx, cudaError_t e, const char* where) {
+    if (e == cudaSuccess) return QB_OK;
+    const int code = (e == cudaErrorMemoryAllocation) ? QB_ERR_NOMEM : QB_ERR_CUDA;
+    return qb_set_error(ctx, code, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define QB_TRY(expr)                                  \
+    do {                                              \
+        const int _rc = (expr);                       \
+        if (_rc != QB_OK) return _rc;                 \
+    } while (0)
+#define QB_CUDA(ctx, call) QB_TRY(qb_cuda_check((ctx), (call), #call))
+
+// ---------------------------------------------------------------------------
+// Boys table: F_m(T_k), T_k = k/16, by the power series
+//   F_m(T) = e^{-T} sum_i (2T)^i / ((2m+1)(2m+3)...(2m+2i+1))
+// in extended precision, then stored as the Taylor coefficients of qb_common.cuh.
+std::vector<double> qb_build_boys_table() {
+    const int NM = QB_BOYS_NM, NJ = QB_BOYS_NJ, MT = NM + NJ - 1;
+    std::vector<double> tab((size_t)QB_BOYS_NROW * NM * NJ);
+    std::vector<long double> F(MT + 1);
+    long double fact[NJ];
+    fact[0] = 1.0L;
+    for (int j = 1; j < NJ; ++j) fact[j] = fact[j - 1] * j;
+    for (int k = 0; k < QB_BOYS_NROW; ++k) {
+        const long double T = (long double)k / 16.0L;
+        // top order by the series, then downward recursion (stable)
+        long double term = 1.0L / (2 * MT + 1), sum = term;
+        for (int i = 1; i < 100000; ++i) {
+            term *= 2.0L * T / (2 * MT + 2 * i + 1);
+            sum += term;
+            if (term < sum * 1e-30L) break;
+        }
+        const long double ex = expl(-T);
+        F[MT] = ex * sum;
+        for (int m = MT; m > 0; --m) F[m - 1] = (2.0L * T * F[m] + ex) / (2 * m - 1);
+        for (int m = 0; m < NM; ++m)
+            for (int j = 0; j < NJ; ++j) {
+                const long double c = F[m + j] / fact[j] * ((j & 1) ? -1.0L : 1.0L);
+                tab[((size_t)k * NM + m) * NJ + j] = (double)c;
+            }
+    }
+    return tab;
+}
+
+// ---------------------------------------------------------------------------
+static bool same_vec(const std::vector<double>& a, const double* b, size_t n) {
+    return a.size() == n && (n == 0 || std::memcmp(a.data(), b, n * sizeof(double)) == 0);
+}
+static bool same_vec(const std::vector<int>& a, const int* b, size_t n) {
+    return a.size() == n && (n == 0 || std::memcmp(a.data(), b, n * sizeof(int)) == 0);
+}
+
+static std::vector<std::array<int, 3>> cart_components(int L) {
+    std::vector<std::array<int, 3>> out;
+    for (int i = L; i >= 0; --i)
+        for (int j = L - i; j >= 0; --j) out.push_back({i, j, L - i - j});
+    return out;
+}
+
+// Groups consecutive functions into Cartesian shells: same centre, exponents and
+// primitive count, powers in SubshellXYZs order (src/Lexicons.jl:17-36), and
+// weights that factor as ratio(function) * coefficient(primitive).
+static void detect_shells(qb_ctx* ctx) {
+    ctx->shells.clear();
+    ctx->h_ratio.assign(ctx->nfun, 1.0);
+    ctx->shell_path = true;
+    const int* fp = ctx->h_fp.data();
+    const double* cen = ctx->h_cen.data();
+    const int* ijk = ctx->h_ijk.data();
+    const double* al = ctx->h_alpha.data();
+    const double* w = ctx->h_w.data();
+    int f = 0;
+    while (f < ctx->nfun) {
+        const int p0 = fp[f], K = fp[f + 1] - fp[f];
+        bool ok = K > 0;
+        int L = ok ? ijk[3 * p0] + ijk[3 * p0 + 1] + ijk[3 * p0 + 2] : -1;
+        ok = ok && L <= QB_LMAX_SHELL;
+        std::vector<std::array<int, 3>> comps;
+        if (ok) comps = cart_components(L);
+        const int nc = ok ? (int)comps.size() : 0;
+        ok = ok && f + nc <= ctx->nfun;
+        for (int c = 0; ok && c < nc; ++c) {
+            const int g = f + c, q0 = fp[g];
+            if (fp[g + 1] - q0 != K) { ok = false; break; }
+            const double r = w[p0] != 0.0 ? w[q0] / w[p0] : 0.0;
+            if (w[p0] == 0.0) { ok = false; break; }
+            for (int k = 0; k < K && ok; ++k) {
+                const int pa = p0 + k, pb = q0 + k;
+                if (al[pa] != al[pb]) ok = false;
+                for (int x = 0; x < 3; ++x) {
+                    if (cen[3 * pb + x] != cen[3 * p0 + x]) ok = false;
+                    if (ijk[3 * pb + x] != comps[c][x]) ok = false;
+                }
+                if (w[pa] == 0.0 || std::fabs(w[pb] - r * w[pa]) > 1e-13 * std::fabs(w[pb])) ok = false;
+            }
+            if (ok) ctx->h_ratio[g] = r;
+        }
+        if (!ok) {
+            ctx->shell_path = false;
+            ctx->shells.clear();
+            ctx->h_ratio.assign(ctx->nfun, 1.0);
+            return;
+        }
+        HostShell s;
+        for (int x = 0; x < 3; ++x) s.c[x] = cen[3 * p0 + x];
+        s.L = L;
+        s.K = K;
+        s.prim0 = p0;
+        s.f0 = f;
+        ctx->shells.push_back(s);
+        f += nc;
+    }
+}
+
+int qb_set_basis(qb_ctx* ctx, const qb_basis* b) {
+    if (!ctx || !b || !b->fun_ptr) return qb_set_error(ctx, QB_ERR_ARG, "null basis");
+    if (b->nfun <= 0) return qb_set_error(ctx, QB_ERR_DIM, "basis has no functions");
+    const int nf = b->nfun;
+    if (b->fun_ptr[0] != 0) return qb_set_error(ctx, QB_ERR_ARG, "fun_ptr[0] must be 0");
+    for (int f = 0; f < nf; ++f)
+        if (b->fun_ptr[f + 1] <= b->fun_ptr[f])
+            return qb_set_error(ctx, QB_ERR_ARG, "every function needs at least one primitive");
+    const int np = b->fun_ptr[nf];
+    if (!b->center || !b->ijk || !b->alpha || !b->weight) return qb_set_error(ctx, QB_ERR_ARG, "null basis array");
+    if (ctx->basis_valid && ctx->nfun == nf && same_vec(ctx->h_fp, b->fun_ptr, nf + 1) &&
+        same_vec(ctx->h_cen, b->center, 3 * (size_t)np) && same_vec(ctx->h_ijk, b->ijk, 3 * (size_t)np) &&
+        same_vec(ctx->h_alpha, b->alpha, np) && same_vec(ctx->h_w, b->weight, np))
+        return QB_OK;
+    for (int p = 0; p < np; ++p) {
+        if (!(b->alpha[p] > 0.0) || !std::isfinite(b->alpha[p]) || !std::isfinite(b->weight[p]))
+            return qb_set_error(ctx, QB_ERR_DOMAIN, "exponents must be positive and finite");
+        int L = 0;
+        for (int x = 0; x < 3; ++x) {
+            if (b->ijk[3 * p + x] < 0) return qb_set_error(ctx, QB_ERR_DOMAIN, "negative Cartesian power");
+            if (!std::isfinite(b->center[3 * p + x])) return qb_set_error(ctx, QB_ERR_DOMAIN, "non-finite centre");
+            L += b->ijk[3 * p + x];
+        }
+        if (L > 12) return qb_set_error(ctx, QB_ERR_UNSUPPORTED, "primitive angular momentum above 12");
+    }
+    ctx->basis_valid = false;
+    ctx->pairs_valid = false;
+    ctx->jk_prepared = false;
+    ctx->nfun = nf;
+    ctx->nprim = np;
+    ctx->h_fp.assign(b->fun_ptr, b->fun_ptr + nf + 1);
+    ctx->h_cen.assign(b->center, b->center + 3 * (size_t)np);
+    ctx->h_ijk.assign(b->ijk, b->ijk + 3 * (size_t)np);
+    ctx->h_alpha.assign(b->alpha, b->alpha + np);
+    ctx->h_w.assign(b->weight, b->weight + np);
+    QB_CUDA(ctx, ctx->d_fp.ensure(nf + 1));
+    QB_CUDA(ctx, ctx->d_cen.ensure(3 * (size_t)np));
+    QB_CUDA(ctx, ctx->d_ijk.ensure(3 * (size_t)np));
+    QB_CUDA(ctx, ctx->d_alpha.ensure(np));
+    QB_CUDA(ctx, ctx->d_w.ensure(np));
+    cudaStream_t s = ctx->stream;
+    QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_fp.p, b->fun_ptr, (nf + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+    QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_cen.p, b->center, 3 * np * sizeof(double), cudaMemcpyHostToDevice, s));
+    QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_ijk.p, b->ijk, 3 * np * sizeof(int), cudaMemcpyHostToDevice, s));
+    QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_alpha.p, b->alpha, np * sizeof(double), cudaMemcpyHostToDevice, s));
+    QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_w.p, b->weight, np * sizeof(double), cudaMemcpyHostToDevice, s));
+    detect_shells(ctx);
+    QB_CUDA(ctx, ctx->d_ratio.ensure(nf));
+    QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_ratio.p, ctx->h_ratio.data(), nf * sizeof(double), cudaMemcpyHostToDevice, s));
+    QB_CUDA(ctx, cudaStreamSynchronize(s));
+    ctx->basis_valid = true;
+    return QB_OK;
+}
+
+GenDevBasis qb_gen_basis(qb_ctx* ctx) {
+    return GenDevBasis{ctx->d_fp.p, ctx->d_cen.p, ctx->d_ijk.p, ctx->d_alpha.p, ctx->d_w.p, ctx->nfun};
+}
+
+int qb_check_status(qb_ctx* ctx) {
+    int st = 0;
+    QB_CUDA(ctx, cudaMemcpyAsync(&st, ctx->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    QB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (st != 0) {
+        cudaMemsetAsync(ctx->status.p, 0, sizeof(int), ctx->stream);
+        return qb_set_error(ctx, QB_ERR_UNSUPPORTED, "a kernel met an index beyond its limits (status " +
+                                                         std::to_string(st) + ")");
+    }
+    return QB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Shell pairs and primitive pairs.
+struct PairSlot {
+    int sa, sb, pa, pb;   // shells and shell-primitive indices (into the flattened basis)
+};
+
+__global__ void qb_primpair_kernel(const PairSlot* __restrict__ slots, int n, const double* __restrict__ cen,
+                                   const double* __restrict__ alpha, const double* __restrict__ w,
+                                   PrimPair* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const PairSlot s = slots[k];
+    const double a = alpha[s.pa], b = alpha[s.pb];
+    const double* A = cen + 3 * s.pa;
+    const double* B = cen + 3 * s.pb;
+    const double p = a + b, ip = 1.0 / p;
+    PrimPair r;
+    r.p = p;
+    r.Px = (a * A[0] + b * B[0]) * ip;
+    r.Py = (a * A[1] + b * B[1]) * ip;
+    r.Pz = (a * A[2] + b * B[2]) * ip;
+    r.PAx = r.Px - A[0];
+    r.PAy = r.Py - A[1];
+    r.PAz = r.Pz - A[2];
+    const double dx = A[0] - B[0], dy = A[1] - B[1], dz = A[2] - B[2];
+    const double ab2 = dx * dx + dy * dy + dz * dz;
+    // sqrt(2) * pi^(5/4)
+    const double c0 = 1.4142135623730950488 * 4.1880627323665752;
+    r.K = c0 * w[s.pa] * w[s.pb] * exp(-a * b * ip * ab2) * ip;
+    r.oo2p = 0.5 * ip;
+    r.pad = 0.0;
+    out[k] = r;
+}
+
+static int pc_index(int la, int lb) { return la * (la + 1) / 2 + lb; }
+
+int qb_ensure_pairs(qb_ctx* ctx) {
+    if (ctx->pairs_valid) return QB_OK;
+    if (!ctx->shell_path) return qb_set_error(ctx, QB_ERR_ARG, "basis is not shell-structured");
+    const int ns = (int)ctx->shells.size();
+    const int npc = (QB_LMAX_SHELL + 1) * (QB_LMAX_SHELL + 2) / 2;
+    ctx->npc = npc;
+    // pairs grouped by pair class, A = shell of higher L
+    std::vector<std::vector<ShellPair>> by(npc);
+    std::vector<std::vector<PairSlot>> slots_by(npc);
+    for (int a = 0; a < ns; ++a)
+        for (int b = 0; b <= a; ++b) {
+            const HostShell* A = &ctx->shells[a];
+            const HostShell* B = &ctx->shells[b];
+            if (B->L > A->L) std::swap(A, B);
+            const int pc = pc_index(A->L, B->L);
+            ShellPair sp;
+            sp.fa = A->f0;
+            sp.fb = B->f0;
+            sp.nprim = A->K * B->K;
+            sp.prim0 = 0;   // set after layout
+            sp.ABx = A->c[0] - B->c[0];
+            sp.ABy = A->c[1] - B->c[1];
+            sp.ABz = A->c[2] - B->c[2];
+            sp.Q = 0.0;
+            sp.same = (a == b);
+            sp.pad = (int)slots_by[pc].size();   // local slot offset, replaced below
+            for (int i = 0; i < A->K; ++i)
+                for (int j = 0; j < B->K; ++j)
+                    slots_by[pc].push_back(PairSlot{a, b, A->prim0 + i, B->prim0 + j});
+            by[pc].push_back(sp);
+        }
+    std::vector<ShellPair> pairs;
+    std::vector<PairSlot> slots;
+    for (int pc = 0; pc < npc; ++pc) {
+        ctx->pc_off[pc] = (int)pairs.size();
+        const int base = (int)slots.size();
+        for (auto sp : by[pc]) {
+            sp.prim0 = base + sp.pad;
+            sp.pad = 0;
+            pairs.push_back(sp);
+        }
+        slots.insert(slots.end(), slots_by[pc].begin(), slots_by[pc].end());
+    }
+    ctx->pc_off[npc] = (int)pairs.size();
+    const int npair = (int)pairs.size(), nslot = (int)slots.size();
+    cudaStream_t s = ctx->stream;
+    DevArray<PairSlot> d_slots;
+    QB_CUDA(ctx, d_slots.ensure(nslot));
+    QB_CUDA(ctx, ctx->d_prims.ensure(nslot));
+    QB_CUDA(ctx, ctx->d_pairs.ensure(npair));
+    QB_CUDA(ctx, ctx->d_Q.ensure(npair));
+    QB_CUDA(ctx, cudaMemcpyAsync(d_slots.p, slots.data(), nslot * sizeof(PairSlot), cudaMemcpyHostToDevice, s));
+    QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_pairs.p, pairs.data(), npair * sizeof(ShellPair), cudaMemcpyHostToDevice, s));
+    qb_primpair_kernel<<<(nslot + 127) / 128, 128, 0, s>>>(d_slots.p, nslot, ctx->d_cen.p, ctx->d_alpha.p,
+                                                          ctx->d_w.p, ctx->d_prims.p);
+    QB_CUDA(ctx, cudaGetLastError());
+    // Schwarz factors (generic kernel over the diagonal function quartets of every pair)
+    for (int pc = 0; pc < npc; ++pc) {
+        int la = 0;
+        while ((la + 1) * (la + 2) / 2 <= pc) ++la;
+        const int lb = pc - la * (la + 1) / 2;
+        const int n = ctx->pc_off[pc + 1] - ctx->pc_off[pc];
+        if (qb_gen_schwarz(qb_gen_basis(ctx), ctx->boys.p, ctx->d_pairs.p + ctx->pc_off[pc], n, (la + 1) * (la + 2) / 2,
+                           (lb + 1) * (lb + 2) / 2, ctx->d_Q.p + ctx->pc_off[pc], ctx->status.p, s) != 0)
+            return qb_cuda_check(ctx, cudaGetLastError(), "Schwarz kernel");
+    }
+    QB_TRY(qb_check_status(ctx));
+    std::vector<double> Q(npair);
+    QB_CUDA(ctx, cudaMemcpyAsync(Q.data(), ctx->d_Q.p, npair * sizeof(double), cudaMemcpyDeviceToHost, s));
+    QB_CUDA(ctx, cudaStreamSynchronize(s));
+    d_slots.release();
+    // sort each pair class by descending Q
+    std::vector<ShellPair> sorted(npair);
+    std::vector<double> Qs(npair);
+    std::vector<long long> npref;
+    for (int pc = 0; pc < npc; ++pc) {
+        const int o = ctx->pc_off[pc], n = ctx->pc_off[pc + 1] - o;
+        std::vector<int> idx(n);
+        std::iota(idx.begin(), idx.end(), 0);
+        std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return Q[o + x] > Q[o + y]; });
+        ctx->npref_off[pc] = (int)npref.size();
+        long long acc = 0;
+        for (int k = 0; k < n; ++k) {
+            ShellPair sp = pairs[o + idx[k]];
+            sp.Q = Q[o + idx[k]];
+            sorted[o + k] = sp;
+            Qs[o + k] = sp.Q;
+            npref.push_back(acc);
+            acc += sp.nprim;
+        }
+        npref.push_back(acc);
+    }
+    ctx->npref_off[npc] = (int)npref.size();
+    ctx->h_pairs = sorted;
+    QB_CUDA(ctx, ctx->d_npref.ensure(npref.size()));
+    QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_pairs.p, sorted.data(), npair * sizeof(ShellPair), cudaMemcpyHostToDevice, s));
+    QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_Q.p, Qs.data(), npair * sizeof(double), cudaMemcpyHostToDevice, s));
+    QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_npref.p, npref.data(), npref.size() * sizeof(long long),
+                                 cudaMemcpyHostToDevice, s));
+    // class work-list layout
+    long long off = 0;
+    for (int c = 0; c < ctx->nclass; ++c) {
+        const ClassLaunchers& L = ctx->launch[c];
+        ctx->class_bra[c] = pc_index(L.la, L.lb);
+        ctx->class_ket[c] = pc_index(L.lc, L.ld);
+        ctx->offs_off[c] = off;
+        off += (ctx->pc_off[ctx->class_bra[c] + 1] - ctx->pc_off[ctx->class_bra[c]]) + 1;
+    }
+    ctx->offs_off[ctx->nclass] = off;
+    QB_CUDA(ctx, ctx->d_offs.ensure(off));
+    QB_CUDA(ctx, ctx->d_stats.ensure(2 * QB_MAX_CLASS));
+    QB_CUDA(ctx, cudaStreamSynchronize(s));
+    ctx->pairs_valid = true;
+    return QB_OK;
+}
+
+// ---------------------------------------------------------------------------
+struct CountPlan {
+    int nclass;
+    int bra_off[QB_MAX_CLASS], nbra[QB_MAX_CLASS], ket_off[QB_MAX_CLASS], nket[QB_MAX_CLASS];
+    int same[QB_MAX_CLASS], npref_off[QB_MAX_CLASS];
+    long long offs_off[QB_MAX_CLASS];
+};
+
+// One block per class: per bra pair the number of surviving ket pairs (binary
+// search in the descending Q list), its exclusive prefix sum, and the class
+// totals of shell quartets and primitive quartets.
+__global__ void __launch_bounds__(1024) qb_count_kernel(const CountPlan plan, const ShellPair* __restrict__ pairs,
+                                                        const double* __restrict__ Q,
+                                                        const long long* __restrict__ npref,
+                                                        const double* __restrict__ dmax, double thr,
+                                                        long long* __restrict__ offs, long long* __restrict__ stats) {
+    const int c = blockIdx.x;
+    const int nb = plan.nbra[c], nk = plan.nket[c];
+    const int bo = plan.bra_off[c], ko = plan.ket_off[c];
+    long long* o = offs + plan.offs_off[c];
+    const double dm = dmax ? *dmax : 1.0;
+    const bool all = !(thr > 0.0);
+    __shared__ long long wsum[32];
+    __shared__ long long s_carry, s_pq;
+    if (threadIdx.x == 0) { s_carry = 0; s_pq = 0; }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int base = 0; base < nb; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        long long cnt = 0, pq = 0;
+        if (i < nb) {
+            int hi = nk;
+            if (!all) {
+                const double qi = Q[bo + i];
+                if (!(qi > 0.0) || !(dm > 0.0)) {
+                    hi = 0;
+                } else {
+                    const double t = thr / (dm * qi);
+                    int lo = 0;
+                    hi = nk;
+                    while (lo < hi) {   // first j with Q[j] < t
+                        const int mid = (lo + hi) >> 1;
+                        if (Q[ko + mid] >= t) lo = mid + 1; else hi = mid;
+                    }
+                    hi = lo;
+                }
+            }
+            if (plan.same[c] && hi > i + 1) hi = i + 1;
+            cnt = hi;
+            pq = (long long)pairs[bo + i].nprim * npref[plan.npref_off[c] + hi];
+        }
+        // block-wide inclusive scan of cnt
+        long long v = cnt;
+        for (int d = 1; d < 32; d <<= 1) {
+            const long long y = __shfl_up_sync(0xffffffffu, v, d);
+            if (lane >= d) v += y;
+        }
+        if (lane == 31) wsum[warp] = v;
+        long long pqw = pq;
+        for (int d = 16; d > 0; d >>= 1) pqw += __shfl_down_sync(0xffffffffu, pqw, d);
+        __syncthreads();
+        if (warp == 0) {
+            long long x = lane < nw ? wsum[lane] : 0;
+            for (int d = 1; d < 32; d <<= 1) {
+                const long long y = __shfl_up_sync(0xffffffffu, x, d);
+                if (lane >= d) x += y;
+            }
+            if (lane < nw) wsum[lane] = x;
+        }
+        __syncthreads();
+        const long long before = (warp > 0 ? wsum[warp - 1] : 0) + s_carry;
+        if (i < nb) o[i] = before + v - cnt;
+        if (lane == 0) atomicAdd((unsigned long long*)&s_pq, (unsigned long long)pqw);
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += wsum[nw - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        o[nb] = s_carry;
+        stats[2 * c] = s_carry;
+        stats[2 * c + 1] = s_pq;
+    }
+}
+
+int qb_jk_device(qb_ctx* ctx, const double* dD, double* dJ, double* dK, double thr, cudaStream_t s) {
+    const int n = ctx->nfun;
+    const size_t nn = (size_t)n * n;
+    QB_CUDA(ctx, ctx->d_Dt.ensure(nn));
+    QB_CUDA(ctx, ctx->d_Jp.ensure(nn));
+    QB_CUDA(ctx, ctx->d_Kp.ensure(nn));
+    QB_CUDA(ctx, ctx->d_dmax.ensure(1));
+    QB_CUDA(ctx, cudaMemsetAsync(ctx->d_Jp.p, 0, nn * sizeof(double), s));
+    QB_CUDA(ctx, cudaMemsetAsync(ctx->d_Kp.p, 0, nn * sizeof(double), s));
+    QB_CUDA(ctx, cudaMemsetAsync(ctx->d_dmax.p, 0, sizeof(double), s));
+    const bool shell = ctx->shell_path;
+    qb_density_prescale(s, n, shell ? ctx->d_ratio.p : nullptr, dD, ctx->d_Dt.p, ctx->d_dmax.p);
+    ctx->last_execute_shell = shell;
+    if (!shell) {
+        if (qb_gen_eri(qb_gen_basis(ctx), 1, ctx->boys.p, nullptr, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p,
+                       ctx->status.p, ctx->nsm, s) != 0)
+            return qb_cuda_check(ctx, cudaGetLastError(), "generic J/K launch");
+        qb_jk_finalize(s, n, nullptr, ctx->d_Jp.p, ctx->d_Kp.p, dJ, dK);
+        return qb_cuda_check(ctx, cudaGetLastError(), "J/K finalize");
+    }
+    QB_TRY(qb_ensure_pairs(ctx));
+    CountPlan plan;
+    plan.nclass = ctx->nclass;
+    for (int c = 0; c < ctx->nclass; ++c) {
+        const int X = ctx->class_bra[c], Y = ctx->class_ket[c];
+        plan.bra_off[c] = ctx->pc_off[X];
+        plan.nbra[c] = ctx->pc_off[X + 1] - ctx->pc_off[X];
+        plan.ket_off[c] = ctx->pc_off[Y];
+        plan.nket[c] = ctx->pc_off[Y + 1] - ctx->pc_off[Y];
+        plan.same[c] = (X == Y);
+        plan.npref_off[c] = ctx->npref_off[Y];
+        plan.offs_off[c] = ctx->offs_off[c];
+    }
+    qb_count_kernel<<<ctx->nclass, 1024, 0, s>>>(plan, ctx->d_pairs.p, ctx->d_Q.p, ctx->d_npref.p, ctx->d_dmax.p,
+                                                  thr, ctx->d_offs.p, ctx->d_stats.p);
+    QB_CUDA(ctx, cudaGetLastError());
+    QB_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
+    for (int k = 0; k < QB_NSTREAM; ++k) QB_CUDA(ctx, cudaStreamWaitEvent(ctx->streams[k], ctx->ev_fork, 0));
+    JKArgs args{ctx->d_prims.p, ctx->boys.p, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p, n};
+    int k = 0;
+    for (int c = ctx->nclass - 1; c >= 0; --c) {   // heavy classes first
+        if (plan.nbra[c] == 0 || plan.nket[c] == 0) continue;
+        ClassWork w{ctx->d_pairs.p + plan.bra_off[c], ctx->d_pairs.p + plan.ket_off[c],
+                    ctx->d_offs.p + plan.offs_off[c], plan.nbra[c], plan.same[c]};
+        const int grid = ctx->nsm * std::max(1, ctx->occ[c]);
+        ctx->launch[c].jk(w, args, grid, ctx->streams[k % QB_NSTREAM]);
+        ++k;
+    }
+    QB_CUDA(ctx, cudaGetLastError());
+    for (int j = 0; j < QB_NSTREAM; ++j) {
+        QB_CUDA(ctx, cudaEventRecord(ctx->ev_join[j], ctx->streams[j]));
+        QB_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join[j], 0));
+    }
+    qb_jk_finalize(s, n, ctx->d_ratio.p, ctx->d_Jp.p, ctx->d_Kp.p, dJ, dK);
+    return qb_cuda_check(ctx, cudaGetLastError(), "J/K finalize");
+}
+
+int qb_onebody_device(qb_ctx* ctx, int flags, int nnuc, const double* Z, const double* R, double* dS, double* dT,
+                      double* dV) {
+    cudaStream_t s = ctx->stream;
+    const double* dZ = nullptr;
+    const double* dR = nullptr;
+    if (flags & 4) {
+        if (nnuc <= 0 || !Z || !R) return qb_set_error(ctx, QB_ERR_ARG, "nuclear attraction needs nuclei");
+        for (int c = 0; c < nnuc; ++c)
+            if (!std::isfinite(Z[c]) || !std::isfinite(R[3 * c]) || !std::isfinite(R[3 * c + 1]) ||
+                !std::isfinite(R[3 * c + 2]))
+                return qb_set_error(ctx, QB_ERR_DOMAIN, "non-finite nuclear charge or position");
+        QB_CUDA(ctx, ctx->d_nucZ.ensure(nnuc));
+        QB_CUDA(ctx, ctx->d_nucR.ensure(3 * (size_t)nnuc));
+        QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_nucZ.p, Z, nnuc * sizeof(double), cudaMemcpyHostToDevice, s));
+        QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_nucR.p, R, 3 * nnuc * sizeof(double), cudaMemcpyHostToDevice, s));
+        dZ = ctx->d_nucZ.p;
+        dR = ctx->d_nucR.p;
+    }
+    if (qb_gen_onebody(qb_gen_basis(ctx), flags, nnuc, dZ, dR, ctx->boys.p, dS, dT, dV, ctx->status.p, s) != 0)
+        return qb_cuda_check(ctx, cudaGetLastError(), "one-body kernel");
+    return QB_OK;
+}

@@ -1,0 +1,410 @@
+"""Generator of the shell-quartet ERI class kernels (HGP scheme) for sm_103a.
+
+For every angular-momentum class (la lb | lc ld) of contracted Cartesian shells
+(la >= lb, lc >= ld, bra pair class >= ket pair class, l <= LMAX) it emits a
+straight-line CUDA device function that
+
+  1. loops over the primitive pairs of the bra and ket shell pairs,
+  2. evaluates the Boys function F_m(T), m <= la+lb+lc+ld, from a Taylor table,
+  3. runs the Obara–Saika vertical recursion (bra, then ket with the
+     electron-transfer cross term) only for the intermediates [e0|f0]^(m) that
+     the targets actually need (backward dependency pruning),
+  4. accumulates the contracted [e0|f0]^(0), e = la..la+lb, f = lc..lc+ld,
+  5. applies the horizontal recursion (bra, then ket) once per contracted
+     quartet to produce the (ab|cd) block in SubshellXYZs component order.
+
+This is the algorithm of Head-Gordon & Pople (J. Chem. Phys. 89, 5777 (1988))
+with the Obara–Saika VRR (J. Chem. Phys. 84, 3963 (1986)); the reference
+evaluates the same integrals one Cartesian component at a time with an
+axis-by-axis OS/electron-transfer scheme
+(src/Integration/Engines/GaussianOrbitals.jl:529-663).
+
+The generator also counts the FP64 operations it emits (add/mul = 1 flop,
+fma = 2 flops) per primitive quartet and per contracted quartet and writes
+them to ``flops_table.json``; that table is the algorithmic-work figure of the
+FP64 roofline.
+
+    python gen_eri.py OUTDIR [--lmax 2]
+"""
+import json
+import sys
+from pathlib import Path
+
+LMAX_DEFAULT = 2
+BOYS_TAYLOR = 8          # Taylor terms j = 0..7 of the Boys table
+AXES = "xyz"
+
+
+def comps(L):
+    """SubshellXYZs[L] (src/Lexicons.jl:17-36)."""
+    return [(i, j, L - i - j) for i in range(L, -1, -1) for j in range(L - i, -1, -1)]
+
+
+def ncart(L):
+    return (L + 1) * (L + 2) // 2
+
+
+def pair_classes(lmax):
+    return [(a, b) for a in range(lmax + 1) for b in range(a + 1)]
+
+
+def quartet_classes(lmax):
+    pcs = pair_classes(lmax)
+    out = []
+    for i, bra in enumerate(pcs):
+        for ket in pcs[:i + 1]:
+            out.append(bra + ket)
+    return out
+
+
+def sub(t, i, k=1):
+    return tuple(v - (k if a == i else 0) for a, v in enumerate(t))
+
+
+def add(t, i, k=1):
+    return tuple(v + (k if a == i else 0) for a, v in enumerate(t))
+
+
+def pick_axis(t):
+    """Recursion direction: the axis with the largest power (first on ties)."""
+    best = 0
+    for a in range(3):
+        if t[a] > t[best]:
+            best = a
+    return best
+
+
+class Counter:
+    def __init__(self):
+        self.add = 0
+        self.mul = 0
+        self.fma = 0
+
+    def flops(self):
+        return self.add + self.mul + 2 * self.fma
+
+
+def tname(e):
+    return "".join(str(v) for v in e)
+
+
+class ClassGen:
+    def __init__(self, la, lb, lc, ld):
+        self.la, self.lb, self.lc, self.ld = la, lb, lc, ld
+        self.L = la + lb + lc + ld
+        self.name = f"{la}{lb}{lc}{ld}"
+        self.prim = Counter()     # per primitive quartet
+        self.contr = Counter()    # per contracted quartet (HRR)
+        self.esets = [e for L in range(la, la + lb + 1) for e in comps(L)]
+        self.fsets = [f for L in range(lc, lc + ld + 1) for f in comps(L)]
+
+    # -- VRR dependency analysis ------------------------------------------------
+    def vrr_children(self, node):
+        e, f, m = node
+        if sum(f) > 0:
+            i = pick_axis(f)
+            f1 = sub(f, i)
+            ch = [(e, f1, m), (e, f1, m + 1)]
+            if f1[i] > 0:
+                f2 = sub(f1, i)
+                ch += [(e, f2, m), (e, f2, m + 1)]
+            if e[i] > 0:
+                ch.append((sub(e, i), f1, m + 1))
+            return ch
+        if sum(e) > 0:
+            i = pick_axis(e)
+            e1 = sub(e, i)
+            ch = [(e1, f, m), (e1, f, m + 1)]
+            if e1[i] > 0:
+                e2 = sub(e1, i)
+                ch += [(e2, f, m), (e2, f, m + 1)]
+            return ch
+        return []
+
+    def vrr_nodes(self):
+        targets = [(e, f, 0) for e in self.esets for f in self.fsets]
+        need = set()
+        stack = list(targets)
+        while stack:
+            n = stack.pop()
+            if n in need:
+                continue
+            need.add(n)
+            stack.extend(self.vrr_children(n))
+        order = sorted(need, key=lambda n: (sum(n[0]) + sum(n[1]), sum(n[1]), -n[2], n))
+        return order, targets
+
+    @staticmethod
+    def vname(n):
+        e, f, m = n
+        if sum(e) == 0 and sum(f) == 0:
+            return f"F{m}"
+        return f"v{tname(e)}_{tname(f)}_{m}"
+
+    def emit_vrr(self, out, ind):
+        order, targets = self.vrr_nodes()
+        c = self.prim
+        for n in order:
+            e, f, m = n
+            if sum(e) == 0 and sum(f) == 0:
+                continue
+            nm = self.vname(n)
+            if sum(f) > 0:
+                i = pick_axis(f)
+                ax = AXES[i]
+                f1 = sub(f, i)
+                a0, a1 = self.vname((e, f1, m)), self.vname((e, f1, m + 1))
+                expr = f"fma(QC{ax}, {a0}, WQ{ax} * {a1})"
+                c.mul += 1
+                c.fma += 1
+                if f1[i] > 0:
+                    f2 = sub(f1, i)
+                    b0, b1 = self.vname((e, f2, m)), self.vname((e, f2, m + 1))
+                    expr = f"fma(oo2q_{f1[i]}, fma(-ppq, {b1}, {b0}), {expr})"
+                    c.fma += 2
+                if e[i] > 0:
+                    d1 = self.vname((sub(e, i), f1, m + 1))
+                    expr = f"fma(oo2pq_{e[i]}, {d1}, {expr})"
+                    c.fma += 1
+            else:
+                i = pick_axis(e)
+                ax = AXES[i]
+                e1 = sub(e, i)
+                a0, a1 = self.vname((e1, f, m)), self.vname((e1, f, m + 1))
+                expr = f"fma(PA{ax}, {a0}, WP{ax} * {a1})"
+                c.mul += 1
+                c.fma += 1
+                if e1[i] > 0:
+                    e2 = sub(e1, i)
+                    b0, b1 = self.vname((e2, f, m)), self.vname((e2, f, m + 1))
+                    expr = f"fma(oo2p_{e1[i]}, fma(-qpq, {b1}, {b0}), {expr})"
+                    c.fma += 2
+            out.append(f"{ind}const double {nm} = {expr};")
+        for t in targets:
+            out.append(f"{ind}acc_{tname(t[0])}_{tname(t[1])} += {self.vname(t)};")
+            c.add += 1
+        used_m = sorted({n[2] for n in order if sum(n[0]) == 0 and sum(n[1]) == 0})
+        maxo2p = max([n[0][pick_axis(n[0])] - 1 for n in order if sum(n[1]) == 0 and sum(n[0]) > 0] + [0])
+        maxo2q = max([n[1][pick_axis(n[1])] - 1 for n in order if sum(n[1]) > 0] + [0])
+        maxo2pq = max([n[0][pick_axis(n[1])] for n in order if sum(n[1]) > 0] + [0])
+        return used_m, maxo2p, maxo2q, maxo2pq
+
+    # -- HRR ---------------------------------------------------------------------
+    def emit_hrr(self, out, ind):
+        c = self.contr
+        la, lb, lc, ld = self.la, self.lb, self.lc, self.ld
+        # bra HRR for every ket target f: (a,b|f) from (e,0|f)
+        def bra_nodes(a_list):
+            need = set()
+            stack = list(a_list)
+            while stack:
+                n = stack.pop()
+                if n in need:
+                    continue
+                need.add(n)
+                a, b = n
+                if sum(b) > 0:
+                    i = pick_axis(b)
+                    stack += [(add(a, i), sub(b, i)), (a, sub(b, i))]
+            return sorted(need, key=lambda n: (sum(n[1]), n))
+
+        bra_t = [(a, b) for a in comps(la) for b in comps(lb)]
+        bnodes = bra_nodes(bra_t)
+
+        def hname(a, b, f):
+            if sum(b) == 0:
+                return f"acc_{tname(a)}_{tname(f)}"
+            return f"h{tname(a)}{tname(b)}_{tname(f)}"
+
+        for f in self.fsets:
+            for (a, b) in bnodes:
+                if sum(b) == 0:
+                    continue
+                i = pick_axis(b)
+                b1 = sub(b, i)
+                out.append(f"{ind}const double {hname(a, b, f)} = fma(AB{AXES[i]}, {hname(a, b1, f)}, "
+                           f"{hname(add(a, i), b1, f)});")
+                c.fma += 1
+
+        # ket HRR for every bra function pair (a,b): (ab|c,d) from (ab|e,0)
+        knodes = bra_nodes([(cc, dd) for cc in comps(lc) for dd in comps(ld)])
+
+        def kname(a, b, cc, dd):
+            if sum(dd) == 0:
+                return hname(a, b, cc)
+            return f"k{tname(a)}{tname(b)}_{tname(cc)}{tname(dd)}"
+
+        for a, b in bra_t:
+            for (cc, dd) in knodes:
+                if sum(dd) == 0:
+                    continue
+                i = pick_axis(dd)
+                d1 = sub(dd, i)
+                out.append(f"{ind}const double {kname(a, b, cc, dd)} = fma(CD{AXES[i]}, "
+                           f"{kname(a, b, cc, d1)}, {kname(a, b, add(cc, i), d1)});")
+                c.fma += 1
+        k = 0
+        for a in comps(la):
+            for b in comps(lb):
+                for cc in comps(lc):
+                    for dd in comps(ld):
+                        out.append(f"{ind}I[{k}] = {kname(a, b, cc, dd)};")
+                        k += 1
+
+    # -- Boys / quartet setup ----------------------------------------------------
+    def emit_quartet_setup(self, out, ind, used_m, o2q, o2pq):
+        c = self.prim
+        M = self.L
+        L = out.append
+        L(f"{ind}const double pq = p + q;")
+        L(f"{ind}const double rs = rsqrt(pq);")
+        L(f"{ind}const double ipq = rs * rs;")
+        L(f"{ind}const double PQx = Px - Qx, PQy = Py - Qy, PQz = Pz - Qz;")
+        L(f"{ind}const double R2 = fma(PQz, PQz, fma(PQy, PQy, PQx * PQx));")
+        L(f"{ind}const double qpq = q * ipq;")
+        L(f"{ind}const double T = (p * qpq) * R2;")
+        L(f"{ind}const double pre = (Kab * Kcd) * rs;")
+        c.add += 4          # pq, PQ
+        c.mul += 2 + 1 + 1 + 2 + 2   # ipq, PQx^2, qpq, T (2), pre (2)
+        c.fma += 2
+        c.add += 8          # rsqrt ~ (counted as 8 flops: approximation + Newton step)
+        if M > 0:
+            L(f"{ind}const double ppq = p * ipq;")
+            L(f"{ind}const double WPx = -qpq * PQx, WPy = -qpq * PQy, WPz = -qpq * PQz;")
+            L(f"{ind}const double WQx = ppq * PQx, WQy = ppq * PQy, WQz = ppq * PQz;")
+            c.mul += 7
+        for k in range(1, o2q + 1):
+            L(f"{ind}const double oo2q_{k} = {float(k)} * oo2q;")
+            c.mul += 1
+        if o2pq:
+            L(f"{ind}const double oo2pq_1 = 0.5 * ipq;")
+            c.mul += 1
+            for k in range(2, o2pq + 1):
+                L(f"{ind}const double oo2pq_{k} = {float(k)} * oo2pq_1;")
+                c.mul += 1
+        # Boys F_0..F_M scaled by the prefactor
+        L(f"{ind}double F[{M + 1}];")
+        L(f"{ind}qb_boys_scaled<{M}>(T, pre, boys_tab, F);")
+        for m in used_m:
+            L(f"{ind}const double F{m} = F[{m}];")
+        # Boys cost as emitted by qb_boys_scaled (qb_common.cuh): Taylor on the
+        # Horner form (7 fma), the prefactor scaling and, for M>2, exp(-T)
+        # (counted as 12 flops) plus the downward recursion (fma+mul per order).
+        if M <= 2:
+            c.fma += 7 * (M + 1)
+            c.mul += M + 1
+        else:
+            c.fma += 7 + M
+            c.mul += 2 + 1 + M
+            c.add += 12
+
+    def generate(self):
+        la, lb, lc, ld = self.la, self.lb, self.lc, self.ld
+        na, nb, nc, nd = ncart(la), ncart(lb), ncart(lc), ncart(ld)
+        nint = na * nb * nc * nd
+        body = []
+        ind = "      "
+        used_m, o2p, o2q, o2pq = self.emit_vrr(body, ind + "  ")
+        setup = []
+        self.emit_quartet_setup(setup, ind + "  ", used_m, o2q, o2pq)
+        hrr = []
+        self.emit_hrr(hrr, "  ")
+        o = []
+        o.append(f"// class ({la}{lb}|{lc}{ld}): {len(self.esets)}x{len(self.fsets)} contracted "
+                 f"[e0|f0], {nint} integrals")
+        o.append(f"template <> struct EriClass<{la}, {lb}, {lc}, {ld}> {{")
+        o.append(f"  static constexpr int NA = {na}, NB = {nb}, NC = {nc}, ND = {nd}, NINT = {nint};")
+        o.append("  static __device__ __forceinline__ void block(")
+        o.append("      const PrimPair* __restrict__ bp, int nbp, const PrimPair* __restrict__ kp, int nkp,")
+        o.append("      double ABx, double ABy, double ABz, double CDx, double CDy, double CDz,")
+        o.append("      const double* __restrict__ boys_tab, double (&I)[NINT]) {")
+        for e in self.esets:
+            for f in self.fsets:
+                o.append(f"  double acc_{tname(e)}_{tname(f)} = 0.0;")
+        o.append("  for (int ib = 0; ib < nbp; ++ib) {")
+        o.append("    const PrimPair B = qb_load_pair(bp + ib);")
+        o.append("    const double p = B.p, Px = B.Px, Py = B.Py, Pz = B.Pz, Kab = B.K;")
+        if la + lb > 0:
+            o.append("    const double PAx = B.PAx, PAy = B.PAy, PAz = B.PAz;")
+        if o2p:
+            o.append("    const double oo2p = B.oo2p;")
+            for k in range(1, o2p + 1):
+                o.append(f"    const double oo2p_{k} = {float(k)} * oo2p;")
+        o.append("    for (int ik = 0; ik < nkp; ++ik) {")
+        o.append("      const PrimPair Kt = qb_load_pair(kp + ik);")
+        o.append("      const double q = Kt.p, Qx = Kt.Px, Qy = Kt.Py, Qz = Kt.Pz, Kcd = Kt.K;")
+        if lc + ld > 0:
+            o.append("      const double QCx = Kt.PAx, QCy = Kt.PAy, QCz = Kt.PAz;")
+        if o2q:
+            o.append("      const double oo2q = Kt.oo2p;")
+        o.append("      {")
+        o += setup
+        o += body
+        o.append("      }")
+        o.append("    }")
+        o.append("  }")
+        o += hrr
+        o.append("  }")
+        o.append("};")
+        # the bra oo2p multiples are per bra primitive pair: amortised over the ket loop
+        return "\n".join(o)
+
+
+HEADER = """// GENERATED by gen_eri.py -- do not edit.
+#pragma once
+#include "qb_common.cuh"
+"""
+
+
+def main(outdir, lmax=LMAX_DEFAULT):
+    outdir = Path(outdir)
+    outdir.mkdir(parents=True, exist_ok=True)
+    table = {}
+    files = []
+    for cls in quartet_classes(lmax):
+        g = ClassGen(*cls)
+        code = g.generate()
+        name = g.name
+        (outdir / f"eri_class_{name}.cuh").write_text(HEADER + code + "\n")
+        la, lb, lc, ld = cls
+        cu = [f'// GENERATED by gen_eri.py -- do not edit.',
+              f'#include "eri_class_{name}.cuh"', '#include "eri_kernels.cuh"',
+              f'QB_DEFINE_LAUNCHERS({la}, {lb}, {lc}, {ld})',
+              f"ClassLaunchers qb_class_{name}() {{ return {{qb_jk_launch_{name}, qb_occ_{name}, "
+              f"{la}, {lb}, {lc}, {ld}}}; }}"]
+        (outdir / f"eri_class_{name}.cu").write_text("\n".join(cu) + "\n")
+        files.append(name)
+        table[name] = {"prim_flops": g.prim.flops(), "contr_flops": g.contr.flops(),
+                       "nint": ncart(cls[0]) * ncart(cls[1]) * ncart(cls[2]) * ncart(cls[3]),
+                       "jk_flops_per_int": 12, "vrr_nodes": len(g.vrr_nodes()[0])}
+    disp = ['// GENERATED by gen_eri.py -- do not edit.', '#include "eri_kernels.cuh"']
+    disp += [f"ClassLaunchers qb_class_{n}();" for n in files]
+    disp.append(f"extern const int QB_NCLASS = {len(files)};")
+    disp.append(f"extern const int QB_LMAX_SHELL = {lmax};")
+    disp.append("extern const double QB_CLASS_PRIM_FLOPS[] = {" +
+                ", ".join(f"{table[n]['prim_flops']}.0" for n in files) + "};")
+    disp.append("extern const double QB_CLASS_CONTR_FLOPS[] = {" +
+                ", ".join(f"{table[n]['contr_flops'] + 12 * table[n]['nint']}.0" for n in files) + "};")
+    disp.append("extern const int QB_CLASS_NINT[] = {" + ", ".join(str(table[n]['nint']) for n in files) + "};")
+    disp.append("void qb_get_class_launchers(ClassLaunchers* out) {")
+    disp += [f"  out[{k}] = qb_class_{n}();" for k, n in enumerate(files)]
+    disp.append("}")
+    (outdir / "eri_dispatch.cu").write_text("\n".join(disp) + "\n")
+    (outdir / "eri_classes.json").write_text(json.dumps({"lmax": lmax, "classes": files}, indent=1))
+    return table
+
+
+if __name__ == "__main__":
+    args = sys.argv[1:]
+    lmax = LMAX_DEFAULT
+    if "--lmax" in args:
+        k = args.index("--lmax")
+        lmax = int(args[k + 1])
+        del args[k:k + 2]
+    tab = main(args[0] if args else "gen", lmax)
+    flops_out = Path(__file__).with_name("flops_table.json")
+    if "--write-flops" in sys.argv:
+        flops_out.write_text(json.dumps({"unit": "FP64 flops (add/mul 1, fma 2)", "lmax": lmax,
+                                         "classes": tab}, indent=1))
+    for k, v in tab.items():
+        print(k, v)

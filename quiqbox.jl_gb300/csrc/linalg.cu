@@ -1,0 +1,428 @@
+// Dense FP64 kernels of the SCF driver: GEMM, Jacobi eigensolver, reductions,
+// the J/K finalisation and the DIIS coefficient solve.
+#include <cuda_runtime.h>
+#include "qb_internal.h"
+
+// ---------------------------------------------------------------------------
+// C = alpha op(A) op(B) + beta C, column-major, 32x32 tiles in shared memory,
+// each thread computing a 2x2 block.
+#define GT 32
+__global__ void qb_gemm_kernel(int tA, int tB, int m, int n, int k, double alpha, const double* __restrict__ A,
+                               int lda, const double* __restrict__ B, int ldb, double beta, double* C, int ldc) {
+    __shared__ double As[GT][GT + 1];
+    __shared__ double Bs[GT][GT + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y;   // 16 x 16
+    const int row0 = blockIdx.x * GT, col0 = blockIdx.y * GT;
+    double acc[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+    for (int kk = 0; kk < k; kk += GT) {
+        for (int r = ty; r < GT; r += 16)
+            for (int c = tx; c < GT; c += 16) {
+                // As[r][c] = op(A)(row0 + r, kk + c); Bs[r][c] = op(B)(kk + r, col0 + c)
+                const int ar = row0 + r, ac = kk + c;
+                double av = 0.0;
+                if (ar < m && ac < k) av = tA ? A[ac + (size_t)lda * ar] : A[ar + (size_t)lda * ac];
+                As[r][c] = av;
+                const int br = kk + r, bc = col0 + c;
+                double bv = 0.0;
+                if (br < k && bc < n) bv = tB ? B[bc + (size_t)ldb * br] : B[br + (size_t)ldb * bc];
+                Bs[r][c] = bv;
+            }
+        __syncthreads();
+#pragma unroll 8
+        for (int q = 0; q < GT; ++q) {
+            const double a0 = As[tx][q], a1 = As[tx + 16][q];
+            const double b0 = Bs[q][ty], b1 = Bs[q][ty + 16];
+            acc[0][0] = fma(a0, b0, acc[0][0]);
+            acc[0][1] = fma(a0, b1, acc[0][1]);
+            acc[1][0] = fma(a1, b0, acc[1][0]);
+            acc[1][1] = fma(a1, b1, acc[1][1]);
+        }
+        __syncthreads();
+    }
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) {
+            const int r = row0 + tx + 16 * i, c = col0 + ty + 16 * j;
+            if (r < m && c < n) {
+                double* dst = C + r + (size_t)ldc * c;
+                *dst = alpha * acc[i][j] + (beta == 0.0 ? 0.0 : beta * *dst);
+            }
+        }
+}
+
+void qb_gemm(cudaStream_t s, int transA, int transB, int m, int n, int k, double alpha, const double* A, int lda,
+             const double* B, int ldb, double beta, double* C, int ldc) {
+    dim3 block(16, 16), grid((m + GT - 1) / GT, (n + GT - 1) / GT);
+    qb_gemm_kernel<<<grid, block, 0, s>>>(transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+
+// ---------------------------------------------------------------------------
+// Cyclic two-sided Jacobi eigensolver (one thread block, matrix in global
+// memory / L2), parallel round-robin ordering: each round rotates n/2 disjoint
+// (p, q) planes.  At most 60 sweeps; status bit 2 is set if it did not reach
+// off(A)^2 <= 1e-30 ||A||^2.  Eigenvalues ascending, eigenvectors in columns.
+#define QB_EIGH_MAXN 1024
+__global__ void __launch_bounds__(1024) qb_jacobi_kernel(int n, double* A, double* V, double* w, double* wtmp,
+                                                         double* Vtmp, int* status) {
+    __shared__ double cs[QB_EIGH_MAXN / 2], sn[QB_EIGH_MAXN / 2];
+    __shared__ int pp[QB_EIGH_MAXN / 2], qq[QB_EIGH_MAXN / 2];
+    __shared__ int pos[QB_EIGH_MAXN];
+    __shared__ double red[32];
+    __shared__ int done;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int m = n + (n & 1);
+    const int half = m / 2;
+    for (int i = tid; i < n * n; i += nt) V[i] = ((i % n) == (i / n)) ? 1.0 : 0.0;
+    if (tid == 0) done = 0;
+    __syncthreads();
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        // convergence test
+        double off = 0.0, tot = 0.0;
+        for (int i = tid; i < n * n; i += nt) {
+            const double a = A[i];
+            tot += a * a;
+            if ((i % n) != (i / n)) off += a * a;
+        }
+        for (int d = 16; d > 0; d >>= 1) {
+            off += __shfl_down_sync(0xffffffffu, off, d);
+            tot += __shfl_down_sync(0xffffffffu, tot, d);
+        }
+        if ((tid & 31) == 0) { red[tid >> 5] = off; }
+        __syncthreads();
+        if (tid == 0) {
+            double o = 0.0;
+            for (int k = 0; k < (nt + 31) / 32; ++k) o += red[k];
+            red[31] = o;
+        }
+        __syncthreads();
+        const double offt = red[31];
+        __syncthreads();
+        if ((tid & 31) == 0) red[tid >> 5] = tot;
+        __syncthreads();
+        if (tid == 0) {
+            double t = 0.0;
+            for (int k = 0; k < (nt + 31) / 32; ++k) t += red[k];
+            done = (offt <= 1e-30 * t || offt == 0.0) ? 1 : 0;
+        }
+        __syncthreads();
+        if (done) break;
+        if (sweep == 59) {
+            if (tid == 0) atomicOr(status, 2);
+            break;
+        }
+        for (int i = tid; i < m; i += nt) pos[i] = i;
+        __syncthreads();
+        for (int round = 0; round < m - 1; ++round) {
+            for (int k = tid; k < half; k += nt) {
+                int p = pos[k], q = pos[m - 1 - k];
+                if (p > q) { const int t = p; p = q; q = t; }
+                double c = 1.0, s = 0.0;
+                if (q < n) {
+                    const double apq = A[p + (size_t)n * q];
+                    if (fabs(apq) > 1e-300) {
+                        const double theta = (A[q + (size_t)n * q] - A[p + (size_t)n * p]) / (2.0 * apq);
+                        const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                        c = 1.0 / sqrt(t * t + 1.0);
+                        s = t * c;
+                    }
+                }
+                pp[k] = p; qq[k] = q; cs[k] = c; sn[k] = s;
+            }
+            __syncthreads();
+            // columns p, q of A and V
+            for (int idx = tid; idx < half * n; idx += nt) {
+                const int k = idx / n, r = idx % n;
+                const int p = pp[k], q = qq[k];
+                if (q >= n || sn[k] == 0.0) continue;
+                const double c = cs[k], s = sn[k];
+                const double ap = A[r + (size_t)n * p], aq = A[r + (size_t)n * q];
+                A[r + (size_t)n * p] = c * ap - s * aq;
+                A[r + (size_t)n * q] = s * ap + c * aq;
+                const double vp = V[r + (size_t)n * p], vq = V[r + (size_t)n * q];
+                V[r + (size_t)n * p] = c * vp - s * vq;
+                V[r + (size_t)n * q] = s * vp + c * vq;
+            }
+            __syncthreads();
+            // rows p, q of A
+            for (int idx = tid; idx < half * n; idx += nt) {
+                const int k = idx / n, col = idx % n;
+                const int p = pp[k], q = qq[k];
+                if (q >= n || sn[k] == 0.0) continue;
+                const double c = cs[k], s = sn[k];
+                const double ap = A[p + (size_t)n * col], aq = A[q + (size_t)n * col];
+                A[p + (size_t)n * col] = c * ap - s * aq;
+                A[q + (size_t)n * col] = s * ap + c * aq;
+            }
+            __syncthreads();
+            if (tid == 0) {   // rotate positions 1..m-1
+                const int last = pos[m - 1];
+                for (int i = m - 1; i > 1; --i) pos[i] = pos[i - 1];
+                pos[1] = last;
+            }
+            __syncthreads();
+        }
+    }
+    // ascending order (stable by index)
+    for (int i = tid; i < n; i += nt) wtmp[i] = A[i + (size_t)n * i];
+    __syncthreads();
+    for (int i = tid; i < n; i += nt) {
+        const double wi = wtmp[i];
+        int r = 0;
+        for (int j = 0; j < n; ++j) {
+            const double wj = wtmp[j];
+            r += (wj < wi) || (wj == wi && j < i);
+        }
+        w[r] = wi;
+        for (int row = 0; row < n; ++row) Vtmp[row + (size_t)n * r] = V[row + (size_t)n * i];
+    }
+    __syncthreads();
+    for (int i = tid; i < n * n; i += nt) V[i] = Vtmp[i];
+}
+
+// w (n), V (n x n) from symmetric A; work needs 2 n^2 + n doubles.
+int qb_eigh(cudaStream_t s, int n, const double* A, double* w, double* V, double* work, int* status) {
+    if (n > QB_EIGH_MAXN) return -1;
+    double* Aw = work;
+    double* Vt = work + (size_t)n * n;
+    double* wt = work + 2 * (size_t)n * n;
+    cudaMemcpyAsync(Aw, A, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    const int threads = n <= 32 ? 64 : (n <= 128 ? 256 : 1024);
+    qb_jacobi_kernel<<<1, threads, 0, s>>>(n, Aw, V, w, wt, Vt, status);
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+__global__ void qb_axpby_kernel(long long n, double a, const double* x, double b, const double* y, double* z) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) z[i] = a * x[i] + (y ? b * y[i] : 0.0);
+}
+void qb_axpby(cudaStream_t s, long long n, double a, const double* x, double b, const double* y, double* z) {
+    if (n > 0) qb_axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, a, x, b, y, z);
+}
+
+__global__ void qb_fill_kernel(long long n, double v, double* x) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = v;
+}
+void qb_fill(cudaStream_t s, long long n, double v, double* x) {
+    if (n > 0) qb_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, v, x);
+}
+
+// Deterministic single-block dot product.
+__global__ void __launch_bounds__(1024) qb_dot_kernel(long long n, const double* x, const double* y, double* out) {
+    __shared__ double red[32];
+    double acc = 0.0;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) acc = fma(x[i], y[i], acc);
+    for (int d = 16; d > 0; d >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, d);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+        *out = t;
+    }
+}
+void qb_dot(cudaStream_t s, long long n, const double* x, const double* y, double* out) {
+    qb_dot_kernel<<<1, 1024, 0, s>>>(n, x, y, out);
+}
+
+// A[i,j] = A[j,i] for i > j: the upper triangle wins (Hermitian(A) in the reference).
+__global__ void qb_symmetrize_upper_kernel(int n, double* A) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i < n && i > j) A[i + (size_t)n * j] = A[j + (size_t)n * i];
+}
+void qb_symmetrize_upper(cudaStream_t s, int n, double* A) {
+    dim3 grid((n + 127) / 128, n);
+    qb_symmetrize_upper_kernel<<<grid, 128, 0, s>>>(n, A);
+}
+
+// Flip the sign of every column whose first entry is negative (HartreeFock.jl:51-53).
+__global__ void qb_sign_kernel(int n, double* C) {
+    const int j = blockIdx.x;
+    const bool flip = C[(size_t)n * j] < 0.0;
+    if (!flip) return;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) C[i + (size_t)n * j] = -C[i + (size_t)n * j];
+}
+void qb_scale_columns_sign(cudaStream_t s, int n, double* C) { qb_sign_kernel<<<n, 128, 0, s>>>(n, C); }
+
+// out = U diag(f(w)) U^T, f = w^-1/2 (kind 0), w^1/2 (kind 1), 1/w (kind 2); work n x n.
+__global__ void qb_scale_cols_kernel(int n, const double* U, const double* w, int kind, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= n) return;
+    const double x = w[j];
+    const double f = kind == 0 ? 1.0 / sqrt(x) : (kind == 1 ? sqrt(x) : 1.0 / x);
+    out[i + (size_t)n * j] = U[i + (size_t)n * j] * f;
+}
+void qb_diag_func(cudaStream_t s, int n, const double* U, const double* w, int kind, double* out, double* work) {
+    dim3 grid((n + 127) / 128, n);
+    qb_scale_cols_kernel<<<grid, 128, 0, s>>>(n, U, w, kind, work);
+    qb_gemm(s, 0, 1, n, n, n, 1.0, work, n, U, n, 0.0, out, n);
+}
+
+// J = r r^T o (Jp + Jp^T)/4,  K = r r^T o (Kp + Kp^T)/8  (r = per-function ratios, or 1)
+__global__ void qb_jk_finalize_kernel(int n, const double* __restrict__ r, const double* __restrict__ Jp,
+                                      const double* __restrict__ Kp, double* J, double* K) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= n) return;
+    const size_t a = i + (size_t)n * j, b = j + (size_t)n * i;
+    const double s = r ? r[i] * r[j] : 1.0;
+    if (J) J[a] = s * 0.25 * (Jp[a] + Jp[b]);
+    if (K) K[a] = s * 0.125 * (Kp[a] + Kp[b]);
+}
+void qb_jk_finalize(cudaStream_t s, int n, const double* ratio, const double* Jp, const double* Kp, double* J,
+                    double* K) {
+    dim3 grid((n + 127) / 128, n);
+    qb_jk_finalize_kernel<<<grid, 128, 0, s>>>(n, ratio, Jp, Kp, J, K);
+}
+
+// Dt = r r^T o D and dmax = max |D_ij| (non-negative doubles order like their bit patterns).
+__global__ void qb_prescale_kernel(int n, const double* __restrict__ r, const double* __restrict__ D, double* Dt,
+                                   unsigned long long* dmax) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    double a = 0.0;
+    if (i < n) {
+        const size_t k = i + (size_t)n * j;
+        const double v = D[k];
+        Dt[k] = r ? r[i] * r[j] * v : v;
+        a = fabs(v);
+    }
+    for (int d = 16; d > 0; d >>= 1) a = fmax(a, __shfl_down_sync(0xffffffffu, a, d));
+    if ((threadIdx.x & 31) == 0) atomicMax(dmax, (unsigned long long)__double_as_longlong(a));
+}
+void qb_density_prescale(cudaStream_t s, int n, const double* ratio, const double* D, double* Dt, double* dmax) {
+    dim3 grid((n + 127) / 128, n);
+    qb_prescale_kernel<<<grid, 128, 0, s>>>(n, ratio, D, Dt, reinterpret_cast<unsigned long long*>(dmax));
+}
+
+// Generalised Wolfsberg–Helmholz one-body matrix: 3 S_ij (H_ii + H_jj) / 8 (HartreeFock.jl:235-254)
+__global__ void qb_gwh_kernel(int n, const double* S, const double* H, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= n) return;
+    out[i + (size_t)n * j] = 3.0 * S[i + (size_t)n * j] * (H[i + (size_t)n * i] + H[j + (size_t)n * j]) / 8.0;
+}
+void qb_gwh(cudaStream_t s, int n, const double* S, const double* H, double* out) {
+    dim3 grid((n + 127) / 128, n);
+    qb_gwh_kernel<<<grid, 128, 0, s>>>(n, S, H, out);
+}
+
+// out = sum_i c[i] * mats[i]  (mats: device array of m device pointers)
+__global__ void qb_lincomb_kernel(long long len, int m, const double* const* mats, const double* c, double* out) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= len) return;
+    double acc = 0.0;
+    for (int i = 0; i < m; ++i) acc = fma(c[i], mats[i][k], acc);
+    out[k] = acc;
+}
+void qb_lincomb(cudaStream_t s, long long len, int m, const double* const* mats, const double* c, double* out) {
+    if (len > 0) qb_lincomb_kernel<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(len, m, mats, c, out);
+}
+
+// ---------------------------------------------------------------------------
+// DIIS coefficient problem (CMsolver!, HartreeFock.jl:1445-1477): solve
+// [B 1; 1 0][c; l] = [-v; 1]; if `convex` and some c < 0, try the subsystems
+// with index subsets removed (by increasing size, smallest |c| first) until a
+// non-negative solution appears; a singular bordered matrix gets B += 4e-13 I.
+// One thread; m <= 16.  Bounded: at most 64 perturbation rounds.
+#define QB_DIIS_MAX 16
+__device__ double lu_solve_dev(int n, double* A, double* b) {   // A n x n col-major, in place; returns det
+    double det = 1.0;
+    for (int k = 0; k < n; ++k) {
+        int p = k;
+        for (int i = k + 1; i < n; ++i)
+            if (fabs(A[i + n * k]) > fabs(A[p + n * k])) p = i;
+        if (A[p + n * k] == 0.0) return 0.0;
+        if (p != k) {
+            for (int j = 0; j < n; ++j) { const double t = A[k + n * j]; A[k + n * j] = A[p + n * j]; A[p + n * j] = t; }
+            const double t = b[k]; b[k] = b[p]; b[p] = t;
+            det = -det;
+        }
+        const double pv = A[k + n * k];
+        det *= pv;
+        for (int i = k + 1; i < n; ++i) {
+            const double f = A[i + n * k] / pv;
+            A[i + n * k] = f;
+            for (int j = k + 1; j < n; ++j) A[i + n * j] -= f * A[k + n * j];
+            b[i] -= f * b[k];
+        }
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        double s = b[i];
+        for (int j = i + 1; j < n; ++j) s -= A[i + n * j] * b[j];
+        b[i] = s / A[i + n * i];
+    }
+    return det;
+}
+
+__global__ void qb_diis_kernel(int m, int convex, const double* Bin, const double* v, double* c, int* status) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int M = m + 1;
+    double B[QB_DIIS_MAX * QB_DIIS_MAX];
+    double A[(QB_DIIS_MAX + 1) * (QB_DIIS_MAX + 1)], W[(QB_DIIS_MAX + 1) * (QB_DIIS_MAX + 1)];
+    double b[QB_DIIS_MAX + 1], x[QB_DIIS_MAX + 1];
+    for (int i = 0; i < m * m; ++i) B[i] = Bin[i];
+    for (int round = 0; round < 64; ++round) {
+        for (int guard = 0; guard < 64; ++guard) {
+            for (int j = 0; j < M; ++j)
+                for (int i = 0; i < M; ++i)
+                    A[i + M * j] = (i < m && j < m) ? B[i + m * j] : ((i == m && j == m) ? 0.0 : 1.0);
+            for (int i = 0; i < M * M; ++i) W[i] = A[i];
+            for (int i = 0; i < M; ++i) x[i] = 0.0;
+            if (lu_solve_dev(M, W, x) != 0.0) break;
+            for (int i = 0; i < m; ++i) B[i + m * i] += 4e-13;
+        }
+        for (int i = 0; i < m; ++i) b[i] = -v[i];
+        b[m] = 1.0;
+        for (int i = 0; i < M * M; ++i) W[i] = A[i];
+        for (int i = 0; i < M; ++i) x[i] = b[i];
+        lu_solve_dev(M, W, x);
+        bool neg = false;
+        for (int i = 0; i < m; ++i) { c[i] = x[i]; neg |= x[i] < 0.0; }
+        if (!convex || !neg) return;
+        int perm[QB_DIIS_MAX];
+        for (int i = 0; i < m; ++i) perm[i] = i;
+        for (int i = 1; i < m; ++i) {   // stable insertion sort by |c|
+            const int t = perm[i];
+            int j = i - 1;
+            while (j >= 0 && fabs(c[perm[j]]) > fabs(c[t])) { perm[j + 1] = perm[j]; --j; }
+            perm[j + 1] = t;
+        }
+        for (int sz = 1; sz <= m; ++sz) {
+            int comb[QB_DIIS_MAX];
+            for (int t = 0; t < sz; ++t) comb[t] = t;
+            while (true) {
+                bool drop[QB_DIIS_MAX + 1];
+                for (int i = 0; i <= m; ++i) drop[i] = false;
+                for (int t = 0; t < sz; ++t) drop[perm[comb[t]]] = true;
+                int keep[QB_DIIS_MAX + 1], k = 0;
+                for (int i = 0; i <= m; ++i)
+                    if (!drop[i]) keep[k++] = i;
+                for (int jj = 0; jj < k; ++jj) {
+                    x[jj] = b[keep[jj]];
+                    for (int ii = 0; ii < k; ++ii) W[ii + k * jj] = A[keep[ii] + M * keep[jj]];
+                }
+                if (lu_solve_dev(k, W, x) != 0.0) {
+                    bool bad = false;
+                    double cl[QB_DIIS_MAX];
+                    for (int i = 0; i < m; ++i) cl[i] = 0.0;
+                    for (int jj = 0; jj < k - 1; ++jj) cl[keep[jj]] = x[jj];
+                    for (int i = 0; i < m; ++i) { c[i] = cl[i]; bad |= cl[i] < 0.0; }
+                    if (!bad) return;
+                }
+                int pos = sz - 1;
+                while (pos >= 0 && comb[pos] == m - sz + pos) --pos;
+                if (pos < 0) break;
+                ++comb[pos];
+                for (int t = pos + 1; t < sz; ++t) comb[t] = comb[t - 1] + 1;
+            }
+        }
+        for (int i = 0; i < m; ++i) B[i + m * i] += 4e-13;
+    }
+    atomicOr(status, 4);
+}
+
+int qb_diis_solve(cudaStream_t s, int m, int convex, const double* B, const double* v, double* c, double* work,
+                  int* status) {
+    (void)work;
+    if (m < 1 || m > QB_DIIS_MAX) return -1;
+    qb_diis_kernel<<<1, 32, 0, s>>>(m, convex, B, v, c, status);
+    return 0;
+}

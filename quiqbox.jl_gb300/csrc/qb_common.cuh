@@ -1,0 +1,145 @@
+// Shared device definitions of the GB300 integral / Hartree–Fock path.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define QB_PI 3.14159265358979323846
+#define QB_SQRT_PI_HALF 0.88622692545275801365   // sqrt(pi)/2
+
+// ---------------------------------------------------------------------------
+// Boys function table.  Row k holds, for T_k = k/16 and every order m, the 8
+// Taylor coefficients c_j = F_{m+j}(T_k) (-1)^j / j!, so that
+//   F_m(T_k + d) = sum_j c_j d^j,  |d| <= 1/32   (relative error < 3e-17).
+// Above T = QB_BOYS_TMAX the asymptotic F_0 = sqrt(pi/T)/2 (erfc(sqrt 40) ~ 1e-19)
+// and the upward recursion F_{m+1} = ((2m+1) F_m - e^{-T}) / (2T) are used.
+#define QB_BOYS_DT_INV 16.0
+#define QB_BOYS_DT 0.0625
+#define QB_BOYS_TMAX 40.0
+#define QB_BOYS_NROW 641      // T_k = 0 .. 40
+#define QB_BOYS_NM 41         // orders m = 0 .. 40
+#define QB_BOYS_NJ 8          // Taylor terms
+
+// Largest total angular momentum of the generic (per-function) kernels.
+#define QB_GEN_LTOT_MAX 32
+
+__device__ __forceinline__ double qb_horner8(const double* __restrict__ c, double d) {
+    const double2 c01 = __ldg(reinterpret_cast<const double2*>(c));
+    const double2 c23 = __ldg(reinterpret_cast<const double2*>(c + 2));
+    const double2 c45 = __ldg(reinterpret_cast<const double2*>(c + 4));
+    const double2 c67 = __ldg(reinterpret_cast<const double2*>(c + 6));
+    double r = fma(c67.y, d, c67.x);
+    r = fma(r, d, c45.y);
+    r = fma(r, d, c45.x);
+    r = fma(r, d, c23.y);
+    r = fma(r, d, c23.x);
+    r = fma(r, d, c01.y);
+    r = fma(r, d, c01.x);
+    return r;
+}
+
+// F[m] = pre * F_m(T) for m = 0..M (compile-time M).
+template <int M>
+__device__ __forceinline__ void qb_boys_scaled(double T, double pre, const double* __restrict__ tab,
+                                               double (&F)[M + 1]) {
+    if (T < QB_BOYS_TMAX) {
+        const int k = __double2int_rn(T * QB_BOYS_DT_INV);
+        const double d = fma(-(double)k, QB_BOYS_DT, T);
+        const double* row = tab + (size_t)k * (QB_BOYS_NM * QB_BOYS_NJ);
+        if (M <= 2) {
+#pragma unroll
+            for (int m = 0; m <= M; ++m) F[m] = pre * qb_horner8(row + m * QB_BOYS_NJ, d);
+        } else {
+            double f = pre * qb_horner8(row + M * QB_BOYS_NJ, d);
+            const double e = pre * exp(-T);
+            const double T2 = T + T;
+            F[M] = f;
+#pragma unroll
+            for (int m = M - 1; m >= 0; --m) {
+                f = fma(T2, f, e) * (1.0 / (2 * m + 1));
+                F[m] = f;
+            }
+        }
+    } else {
+        const double ir = rsqrt(T);
+        double f = pre * QB_SQRT_PI_HALF * ir;
+        F[0] = f;
+        if (M > 0) {
+            const double e = pre * exp(-T);
+            const double i2T = 0.5 * ir * ir;
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                f = fma((double)(2 * m + 1), f, -e) * i2T;
+                F[m + 1] = f;
+            }
+        }
+    }
+}
+
+// Runtime-order variant for the generic kernels: F[0..M], M <= QB_GEN_LTOT_MAX.
+__device__ __forceinline__ void qb_boys_scaled_rt(double T, double pre, const double* __restrict__ tab,
+                                                  int M, double* F) {
+    if (T < QB_BOYS_TMAX) {
+        const int k = __double2int_rn(T * QB_BOYS_DT_INV);
+        const double d = fma(-(double)k, QB_BOYS_DT, T);
+        const double* row = tab + (size_t)k * (QB_BOYS_NM * QB_BOYS_NJ);
+        double f = pre * qb_horner8(row + M * QB_BOYS_NJ, d);
+        F[M] = f;
+        if (M > 0) {
+            const double e = pre * exp(-T);
+            const double T2 = T + T;
+            for (int m = M - 1; m >= 0; --m) {
+                f = fma(T2, f, e) / (double)(2 * m + 1);
+                F[m] = f;
+            }
+        }
+    } else {
+        const double ir = rsqrt(T);
+        double f = pre * QB_SQRT_PI_HALF * ir;
+        F[0] = f;
+        if (M > 0) {
+            const double e = pre * exp(-T);
+            const double i2T = 0.5 * ir * ir;
+            for (int m = 0; m < M; ++m) {
+                f = fma((double)(2 * m + 1), f, -e) * i2T;
+                F[m + 1] = f;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Primitive pair of a shell pair (A, B), A the shell of higher angular momentum:
+//   p = a + b, P = (aA + bB)/p, PA = P - A, oo2p = 1/(2p),
+//   K = sqrt(2) pi^(5/4) c_a c_b exp(-ab/p |A-B|^2) / p
+// so that the primitive ERI prefactor 2 pi^(5/2)/(p q sqrt(p+q)) K_AB K_CD ... equals
+// K_ab K_cd / sqrt(p+q).  80 bytes, 16-byte aligned (five 128-bit loads).
+struct __align__(16) PrimPair {
+    double p, Px, Py, Pz, PAx, PAy, PAz, K, oo2p, pad;
+};
+
+__device__ __forceinline__ PrimPair qb_load_pair(const PrimPair* __restrict__ ptr) {
+    const double2* q = reinterpret_cast<const double2*>(ptr);
+    const double2 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2), d = __ldg(q + 3), e = __ldg(q + 4);
+    PrimPair r;
+    r.p = a.x; r.Px = a.y; r.Py = b.x; r.Pz = b.y; r.PAx = c.x; r.PAy = c.y; r.PAz = d.x; r.K = d.y;
+    r.oo2p = e.x; r.pad = e.y;
+    return r;
+}
+
+// Shell pair (A, B) of a class list.
+struct ShellPair {
+    int fa, fb;        // first basis-function index of shells A and B
+    int prim0, nprim;  // primitive pairs [prim0, prim0+nprim) in the PrimPair table
+    double ABx, ABy, ABz;
+    double Q;          // Schwarz factor sqrt(max |(ab|ab)|)
+    int same;          // A == B (same shell)
+    int pad;
+};
+
+// Generated per class (gen_eri.py): contracted block in SubshellXYZs order,
+// index ((a*NB + b)*NC + c)*ND + d, without the per-function ratios.
+template <int LA, int LB, int LC, int LD>
+struct EriClass;
+
+// Device-side status word: bit flags set by kernels that met an unexpected state.
+#define QB_DEVERR_BAD_INDEX 1

@@ -1,0 +1,63 @@
+"""Host-side mirror of the reference's Julia structures (no GPU)."""
+import math
+
+import numpy as np
+import pytest
+
+
+def test_basis_sizes(qb):
+    # STO-3G: H 1 function, O 5 (1s, 2s, 2p x3); 6-31G: H 2, O 9; cc-pVDZ C: 3s 2p 1d -> 3+6+6
+    assert len(qb.genGaussTypeOrbSeq((0, 0, 0), "H", "STO-3G")) == 1
+    assert len(qb.genGaussTypeOrbSeq((0, 0, 0), "O", "STO-3G")) == 5
+    assert len(qb.genGaussTypeOrbSeq((0, 0, 0), "O", "6-31G")) == 9
+    assert len(qb.genGaussTypeOrbSeq((0, 0, 0), "C", "cc-pVDZ")) == 15
+
+
+def test_missing_basis_is_a_domain_error(qb):
+    with pytest.raises(ValueError, match="DomainError"):
+        qb.genGaussTypeOrbSeq((0, 0, 0), "K", "cc-pVDZ")
+
+
+def test_component_order_and_norm_factor(qb):
+    # SubshellXYZs (src/Lexicons.jl:17-36)
+    assert qb.cartesian_components(2) == [(2, 0, 0), (1, 1, 0), (1, 0, 1), (0, 2, 0), (0, 1, 1), (0, 0, 2)]
+    # normalised s primitive: (2a/pi)^(3/4)
+    a = 0.7
+    assert qb.norm_factor(a, (0, 0, 0)) == pytest.approx((2 * a / math.pi) ** 0.75, rel=1e-15)
+
+
+def test_flatten_weights_bake_normalisation(qb):
+    bs = qb.genGaussTypeOrbSeq((0.1, 0.2, 0.3), "O", "STO-3G")
+    fb = qb.flatten(bs)
+    assert fb.nfun == 5 and list(fb.fun_ptr) == [0, 3, 6, 9, 12, 15]
+    assert np.allclose(fb.center, [0.1, 0.2, 0.3])
+    px = bs[2]
+    w0 = px.effective()[0][1]
+    assert w0 == pytest.approx(px.weights[0])   # no renormalisation by default
+
+
+def test_renormalised_composite_has_unit_norm(qb):
+    from quiqbox_gb300.basis import primitive_overlap
+    g = qb.genGaussTypeOrb((1.0, 1.5, 1.1), [1.5, 0.6], [1.0, 0.8], (1, 0, 0), outerRenormalize=True)
+    eff = g.effective()
+    s = sum(wa * wb * primitive_overlap(pa, pb) for pa, wa in eff for pb, wb in eff)
+    assert s == pytest.approx(1.0, abs=1e-14)
+
+
+def test_nuclear_cluster_sorting_and_repulsion(qb):
+    nuc = qb.NuclearCluster(["O", "H", "H"], [(0, 0, 0), (0.7, 0, 0), (-0.7, 0, 0)])
+    assert nuc.symbols == ["H", "H", "O"] and nuc.coords[0] == (-0.7, 0.0, 0.0)
+    enn = qb.nucRepulsion(nuc)
+    assert enn == pytest.approx(1 / 1.4 + 2 * 8 / 0.7, rel=1e-15)
+    assert qb.prepareSpinConfiguration(nuc) == (5, 5)
+
+
+def test_workload_generator_shapes(qb):
+    from quiqbox_gb300.workloads import random_shell_molecule, random_density
+    atoms, coords, bs = random_shell_molecule(seed=1)
+    assert len(atoms) == 80 and len(bs) == 64 * 4 + 16 * 10
+    c = np.array(coords)
+    d = np.linalg.norm(c[:, None] - c[None], axis=-1) + np.eye(len(c)) * 100
+    assert d.min() >= 1.3 and c.min() >= 0 and c.max() <= 14
+    D = random_density(20)
+    assert np.allclose(D, D.T) and np.linalg.eigvalsh(D).min() > -1e-12
