@@ -46,10 +46,13 @@ def lib():
         L.qbo_prim_eri.restype = _d
         L.qbo_prim_eri.argtypes = [_pd, _d, _pi] * 4
         basis = [_i, _pi, _pd, _pi, _pd, _pd]
-        L.qbo_one_body.argtypes = [_i] + basis + [_i, C.c_void_p, C.c_void_p, _pd]
-        L.qbo_eri_tensor.argtypes = basis + [_pd]
-        L.qbo_eri_list.argtypes = basis + [_i64, _pi, _pd]
-        L.qbo_jk_list.argtypes = basis + [_i64, _pi, _pd, _pd, _pd, _pd, _i]
+        for sfx in ("", "_q"):
+            getattr(L, "qbo_one_body" + sfx).argtypes = [_i] + basis + [_i, C.c_void_p, C.c_void_p, _pd]
+            getattr(L, "qbo_eri_tensor" + sfx).argtypes = basis + [_pd]
+            getattr(L, "qbo_eri_list" + sfx).argtypes = basis + [_i64, _pi, _pd]
+            getattr(L, "qbo_jk_list" + sfx).argtypes = basis + [_i64, _pi, _pd, _pd, _pd, _pd, _i]
+        L.qbo_boys_q.restype = _d
+        L.qbo_boys_q.argtypes = [_d, _i]
         L.qbo_num_threads.restype = _i
         L.qbo_hartree_fock.restype = _i
         L.qbo_hartree_fock.argtypes = basis + [_i, _pd, _pd, _i, _i, _i, _i, C.c_void_p, _i, _pi,
@@ -98,42 +101,53 @@ def prim_eri(p1, p2, p3, p4):
     return lib().qbo_prim_eri(*args)
 
 
-def _one_body(kind, fb, Z=None, R=None):
+def _sfx(exact):
+    return "_q" if exact else ""
+
+
+def boys_exact(x, n):
+    """F_n(x) of the same algorithm evaluated in quad precision."""
+    return lib().qbo_boys_q(float(x), int(n))
+
+
+def _one_body(kind, fb, Z=None, R=None, exact=False):
     n = fb.nfun
+    f = getattr(lib(), "qbo_one_body" + _sfx(exact))
     out = np.zeros((n, n), order="F")
     buf = np.zeros(n * n)
     if Z is None:
-        lib().qbo_one_body(kind, *_b(fb), 0, None, None, buf)
+        f(kind, *_b(fb), 0, None, None, buf)
     else:
         Zc, Rc = _v(Z), _v(R).reshape(-1)
-        lib().qbo_one_body(kind, *_b(fb), len(Zc), Zc.ctypes.data, Rc.ctypes.data, buf)
+        f(kind, *_b(fb), len(Zc), Zc.ctypes.data, Rc.ctypes.data, buf)
     out[:] = buf.reshape((n, n), order="F")
     return out
 
 
-def overlaps(fb):
-    return _one_body(0, fb)
+def overlaps(fb, exact=False):
+    return _one_body(0, fb, exact=exact)
 
 
-def kinetics(fb):
-    return _one_body(1, fb)
+def kinetics(fb, exact=False):
+    return _one_body(1, fb, exact=exact)
 
 
-def nuc_attractions(fb, Z, R):
-    return _one_body(2, fb, Z, R)
+def nuc_attractions(fb, Z, R, exact=False):
+    return _one_body(2, fb, Z, R, exact=exact)
 
 
-def eri_tensor(fb):
+def eri_tensor(fb, exact=False):
+    """(ij|kl) in the reference's canonical orientation; exact=True evaluates in quad precision."""
     n = fb.nfun
     buf = np.zeros(n ** 4)
-    lib().qbo_eri_tensor(*_b(fb), buf)
+    getattr(lib(), "qbo_eri_tensor" + _sfx(exact))(*_b(fb), buf)
     return buf.reshape((n, n, n, n), order="F")
 
 
-def eri_list(fb, quartets):
+def eri_list(fb, quartets, exact=False):
     q = _v(quartets, np.int32).reshape(-1, 4)
     out = np.zeros(len(q))
-    lib().qbo_eri_list(*_b(fb), len(q), q, out)
+    getattr(lib(), "qbo_eri_list" + _sfx(exact))(*_b(fb), len(q), q, out)
     return out
 
 
@@ -148,21 +162,21 @@ def canonical_quartets(n):
     return np.asarray(q, np.int32), np.asarray(g, np.float64)
 
 
-def jk_list(fb, quartets, weights, D, nthreads=0):
+def jk_list(fb, quartets, weights, D, nthreads=0, exact=False):
     """Accumulated (Jp, Kp) for a weighted quartet list (see qbo_jk_list)."""
     n = fb.nfun
     q = _v(quartets, np.int32).reshape(-1, 4)
     Jp = np.zeros(n * n)
     Kp = np.zeros(n * n)
     Dc = np.ascontiguousarray(np.asarray(D, np.float64).reshape(n, n).T).reshape(-1)  # column-major
-    lib().qbo_jk_list(*_b(fb), len(q), q, _v(weights), Dc, Jp, Kp, int(nthreads))
+    getattr(lib(), "qbo_jk_list" + _sfx(exact))(*_b(fb), len(q), q, _v(weights), Dc, Jp, Kp, int(nthreads))
     return Jp.reshape((n, n), order="F"), Kp.reshape((n, n), order="F")
 
 
-def jk(fb, D, nthreads=0):
+def jk(fb, D, nthreads=0, exact=False):
     """Direct J_ij = Σ (ij|kl) D_kl and K_ij = Σ (ik|jl) D_kl over the canonical quartets."""
     q, g = canonical_quartets(fb.nfun)
-    Jp, Kp = jk_list(fb, q, g, D, nthreads)
+    Jp, Kp = jk_list(fb, q, g, D, nthreads, exact)
     return (Jp + Jp.T) / 4, (Kp + Kp.T) / 8
 
 

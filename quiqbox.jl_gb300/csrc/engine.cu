@@ -225,8 +225,8 @@ __global__ void qb_primpair_kernel(const PairSlot* __restrict__ slots, int n, co
     r.PAz = r.Pz - A[2];
     const double dx = A[0] - B[0], dy = A[1] - B[1], dz = A[2] - B[2];
     const double ab2 = dx * dx + dy * dy + dz * dz;
-    // sqrt(2) * pi^(5/4)
-    const double c0 = 1.4142135623730950488 * 4.1880627323665752;
+    // sqrt(2 pi^(5/2)) = sqrt(2) pi^(5/4)
+    const double c0 = 5.9149671727956128778;
     r.K = c0 * w[s.pa] * w[s.pb] * exp(-a * b * ip * ab2) * ip;
     r.oo2p = 0.5 * ip;
     r.pad = 0.0;

@@ -54,11 +54,13 @@ def test_one_body_matrices_vs_oracle(qb, oracle, name):
     from quiqbox_gb300.workloads import H2O_ATOMS, H2O_BENCH_COORDS, molecule_basis
     fb = qb.flatten(molecule_basis(H2O_ATOMS, H2O_BENCH_COORDS, name))
     nuc = qb.NuclearCluster(H2O_ATOMS, H2O_BENCH_COORDS)
-    assert np.abs(qb.overlaps(fb) - oracle.overlaps(fb)).max() < TOL
+    S = qb.overlaps(fb)
+    assert np.abs(S - oracle.overlaps(fb, exact=True)).max() < TOL
+    assert np.abs(S - oracle.overlaps(fb)).max() < TOL
     T = qb.elecKinetics(fb)
-    assert np.abs(T - oracle.kinetics(fb)).max() < TOL
+    assert np.abs(T - oracle.kinetics(fb, exact=True)).max() < TOL
     V = qb.nucAttractions(nuc, fb)
-    assert np.abs(V - oracle.nuc_attractions(fb, nuc.charges, nuc.positions)).max() < 10 * TOL
+    assert np.abs(V - oracle.nuc_attractions(fb, nuc.charges, nuc.positions, exact=True)).max() < TOL
     H = qb.coreHamiltonian(nuc, fb)
     assert np.array_equal(H, T + V)   # coreHamiltonian == elecKinetics + nucAttractions (Interface-test.jl:58)
 
@@ -67,8 +69,8 @@ def test_eri_tensor_vs_oracle_and_symmetry(qb, oracle):
     from quiqbox_gb300.workloads import H2O_ATOMS, H2O_BENCH_COORDS, molecule_basis
     fb = qb.flatten(molecule_basis(H2O_ATOMS, H2O_BENCH_COORDS, "6-31G"))
     E = qb.elecRepulsions(fb)
-    Er = oracle.eri_tensor(fb)
-    assert np.abs(E - Er).max() < TOL
+    assert np.abs(E - oracle.eri_tensor(fb, exact=True)).max() < TOL
+    assert np.abs(E - oracle.eri_tensor(fb)).max() < TOL
     for perm in ((1, 0, 2, 3), (0, 1, 3, 2), (2, 3, 0, 1)):
         assert np.array_equal(E, E.transpose(perm))
 
@@ -83,14 +85,14 @@ def test_high_angular_momentum_and_mixed_centres(qb, oracle):
     c1 = qb.CompositeOrb((p2, p3, p4), (2.0, -1.0, 3.0), renormalize=True)
     bs = [p1, p2, p3, p4, c1]
     fb = qb.flatten(bs)
-    assert np.abs(qb.overlaps(fb) - oracle.overlaps(fb)).max() < TOL
-    assert np.abs(qb.elecKinetics(fb) - oracle.kinetics(fb)).max() < 1e-11
+    assert np.abs(qb.overlaps(fb) - oracle.overlaps(fb, exact=True)).max() < TOL
+    assert np.abs(qb.elecKinetics(fb) - oracle.kinetics(fb, exact=True)).max() < TOL
     Z, R = [3.0, 1.0], [(0.0, 0.0, 0.0), (0.4, -0.3, 0.2)]
-    assert np.abs(qb.nucAttractions(Z, R, fb) - oracle.nuc_attractions(fb, Z, R)).max() < 1e-11
+    assert np.abs(qb.nucAttractions(Z, R, fb) - oracle.nuc_attractions(fb, Z, R, exact=True)).max() < TOL
     q = [(0, 1, 2, 3), (4, 4, 4, 4), (0, 4, 3, 2), (1, 2, 4, 0)]
     g = qb.elecRepulsion_list(fb, q)
-    r = oracle.eri_list(fb, q)
-    assert np.allclose(g, r, rtol=1e-11, atol=TOL)
+    r = oracle.eri_list(fb, q, exact=True)
+    assert np.allclose(g, r, rtol=1e-12, atol=TOL)
 
 
 def test_errors_are_statuses(qb):

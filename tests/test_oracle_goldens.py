@@ -170,3 +170,35 @@ def test_h2o2_631g(qb, oracle, goldens, guess):
                             intervals=(5e-3, 1e-4, h["threshold"]), secondary=(5.0, 5.0))
     assert r["converged"] == 1
     assert abs(r["E_elec"] - h["E_elec"]) < h["tol"]
+
+
+def test_exact_oracle_matches_reference_float64_on_goldens(qb, oracle, goldens):
+    # The quad-precision instance of the same algorithm agrees with the Float64 one on the
+    # reference's LiH goldens and on mpmath's Boys values.
+    fb = _lih(qb, goldens, "coulomb")
+    n = goldens["coulomb"]["lih_nuclei"]
+    V = oracle.nuc_attractions(fb, n["Z"], n["coords"], exact=True)
+    assert np.abs(V.reshape(-1, order="F") - goldens["coulomb"]["lih_V_colmajor"]["values"]).max() < 1e-13
+    E = oracle.eri_tensor(fb, exact=True)
+    assert np.abs(E - oracle.eri_tensor(fb)).max() < 1e-13
+    for p in goldens["boys"]["points"]:
+        assert oracle.boys_exact(p["x"], p["n"]) == pytest.approx(oracle.boys(p["x"], p["n"]), rel=1e-13)
+
+
+def test_reference_electron_transfer_round_off(qb, oracle):
+    # The reference builds all angular momentum on the bra and moves it to the ket by electron
+    # transfer (GaussianOrbitals.jl:529-571), whose -(p/q) factor amplifies round-off when the bra
+    # exponents are much larger than the ket's.  For this (pp|dd) quartet (bra exponents ~45-49,
+    # ket ~1.9) the Float64 result is ~1e-8 away from the exact value in that orientation, and
+    # exact to round-off with bra and ket swapped.
+    from quiqbox_gb300.workloads import random_shell_molecule
+    atoms, coords, bs = random_shell_molecule(n_h=4, n_heavy=2, box=5.0, min_dist=1.0, seed=0)
+    fb = qb.flatten(bs)
+    # functions 27, 17: p shells with exponents (48.9, 0.11, 25.1) and (44.9, 2.45, 1.52);
+    # function 20: a d function with exponents (1.9, 12.7, 2.41)
+    q = [(27, 17, 20, 20), (20, 20, 27, 17)]
+    exact = oracle.eri_list(fb, q, exact=True)
+    f64 = oracle.eri_list(fb, q)
+    assert abs(exact[0] - exact[1]) < 1e-15
+    assert abs(f64[1] - exact[1]) < 1e-14
+    assert abs(f64[0] - exact[0]) > 1e-9
