@@ -82,7 +82,7 @@ void qb_destroy(qb_ctx* ctx) {
     ctx->boys.release(); ctx->status.release();
     ctx->d_fp.release(); ctx->d_ijk.release(); ctx->d_cen.release(); ctx->d_alpha.release(); ctx->d_w.release();
     ctx->d_ratio.release(); ctx->d_pairs.release(); ctx->d_prims.release(); ctx->d_Q.release(); ctx->d_npref.release();
-    ctx->d_offs.release(); ctx->d_stats.release();
+    ctx->d_offs.release(); ctx->d_stats.release(); ctx->d_primcount.release();
     ctx->d_D.release(); ctx->d_Dt.release(); ctx->d_Jp.release(); ctx->d_Kp.release(); ctx->d_J.release();
     ctx->d_K.release(); ctx->d_dmax.release();
     ctx->d_m0.release(); ctx->d_m1.release(); ctx->d_m2.release(); ctx->d_nucZ.release(); ctx->d_nucR.release();
@@ -225,18 +225,21 @@ int qb_jk_get_stats(qb_ctx* ctx, qb_jk_stats* st) {
     cudaGetLastError();
     if (!ctx->shell_path || !ctx->pairs_valid || !ctx->last_execute_shell) return QB_OK;
     std::vector<long long> stats(2 * ctx->nclass);
+    std::vector<unsigned long long> prim(ctx->nclass);
     QB_CUDA(ctx, cudaMemcpy(stats.data(), ctx->d_stats.p, stats.size() * sizeof(long long), cudaMemcpyDeviceToHost));
+    QB_CUDA(ctx, cudaMemcpy(prim.data(), ctx->d_primcount.p, prim.size() * sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost));
     double flops = 0.0;
     for (int c = 0; c < ctx->nclass && c < 32; ++c) {
         st->class_quartets[c] = stats[2 * c];
-        st->class_prim_quartets[c] = stats[2 * c + 1];
+        st->class_prim_quartets[c] = (int64_t)prim[c];
         st->quartets += stats[2 * c];
-        st->prim_quartets += stats[2 * c + 1];
+        st->prim_quartets += (int64_t)prim[c];
         st->class_l[c][0] = ctx->launch[c].la;
         st->class_l[c][1] = ctx->launch[c].lb;
         st->class_l[c][2] = ctx->launch[c].lc;
         st->class_l[c][3] = ctx->launch[c].ld;
-        flops += (double)stats[2 * c + 1] * QB_CLASS_PRIM_FLOPS[c] + (double)stats[2 * c] * QB_CLASS_CONTR_FLOPS[c];
+        flops += (double)prim[c] * QB_CLASS_PRIM_FLOPS[c] + (double)stats[2 * c] * QB_CLASS_CONTR_FLOPS[c];
     }
     st->flops = flops;
     return QB_OK;

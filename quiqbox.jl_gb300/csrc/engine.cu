@@ -207,7 +207,7 @@ struct PairSlot {
 
 __global__ void qb_primpair_kernel(const PairSlot* __restrict__ slots, int n, const double* __restrict__ cen,
                                    const double* __restrict__ alpha, const double* __restrict__ w,
-                                   PrimPair* __restrict__ out) {
+                                   PrimPair* __restrict__ out, unsigned long long* __restrict__ kmax) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const PairSlot s = slots[k];
@@ -231,6 +231,31 @@ __global__ void qb_primpair_kernel(const PairSlot* __restrict__ slots, int n, co
     r.oo2p = 0.5 * ip;
     r.pad = 0.0;
     out[k] = r;
+    atomicMax(kmax, (unsigned long long)__double_as_longlong(fabs(r.K)));
+}
+
+// Per shell pair: sort its primitive pairs by descending |K| and drop those with
+// |K| * max|K| < QB_PRIM_EPS (negligible against every partner); writes the kept count.
+__global__ void qb_primpair_compact_kernel(const ShellPair* __restrict__ pairs, int npair, PrimPair* prims,
+                                           const unsigned long long* __restrict__ kmax_bits, int* __restrict__ nkept) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= npair) return;
+    const ShellPair sp = pairs[k];
+    const double kmax = __longlong_as_double((long long)*kmax_bits);
+    PrimPair* pp = prims + sp.prim0;
+    // insertion sort by |K| (at most a few dozen entries)
+    for (int i = 1; i < sp.nprim; ++i) {
+        const PrimPair x = pp[i];
+        int j = i - 1;
+        while (j >= 0 && fabs(pp[j].K) < fabs(x.K)) {
+            pp[j + 1] = pp[j];
+            --j;
+        }
+        pp[j + 1] = x;
+    }
+    int kept = 0;
+    while (kept < sp.nprim && fabs(pp[kept].K) * kmax >= QB_PRIM_EPS) ++kept;
+    nkept[k] = kept;
 }
 
 static int pc_index(int la, int lb) { return la * (la + 1) / 2 + lb; }
@@ -288,9 +313,23 @@ int qb_ensure_pairs(qb_ctx* ctx) {
     QB_CUDA(ctx, ctx->d_Q.ensure(npair));
     QB_CUDA(ctx, cudaMemcpyAsync(d_slots.p, slots.data(), nslot * sizeof(PairSlot), cudaMemcpyHostToDevice, s));
     QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_pairs.p, pairs.data(), npair * sizeof(ShellPair), cudaMemcpyHostToDevice, s));
+    DevArray<unsigned long long> d_kmax;
+    DevArray<int> d_nkept;
+    QB_CUDA(ctx, d_kmax.ensure(1));
+    QB_CUDA(ctx, d_nkept.ensure(npair));
+    QB_CUDA(ctx, cudaMemsetAsync(d_kmax.p, 0, sizeof(unsigned long long), s));
     qb_primpair_kernel<<<(nslot + 127) / 128, 128, 0, s>>>(d_slots.p, nslot, ctx->d_cen.p, ctx->d_alpha.p,
-                                                          ctx->d_w.p, ctx->d_prims.p);
+                                                          ctx->d_w.p, ctx->d_prims.p, d_kmax.p);
+    qb_primpair_compact_kernel<<<(npair + 127) / 128, 128, 0, s>>>(ctx->d_pairs.p, npair, ctx->d_prims.p, d_kmax.p,
+                                                                  d_nkept.p);
     QB_CUDA(ctx, cudaGetLastError());
+    {
+        std::vector<int> nkept(npair);
+        QB_CUDA(ctx, cudaMemcpyAsync(nkept.data(), d_nkept.p, npair * sizeof(int), cudaMemcpyDeviceToHost, s));
+        QB_CUDA(ctx, cudaStreamSynchronize(s));
+        for (int k = 0; k < npair; ++k) pairs[k].nprim = nkept[k];
+        QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_pairs.p, pairs.data(), npair * sizeof(ShellPair), cudaMemcpyHostToDevice, s));
+    }
     // Schwarz factors (generic kernel over the diagonal function quartets of every pair)
     for (int pc = 0; pc < npc; ++pc) {
         int la = 0;
@@ -346,6 +385,7 @@ int qb_ensure_pairs(qb_ctx* ctx) {
     ctx->offs_off[ctx->nclass] = off;
     QB_CUDA(ctx, ctx->d_offs.ensure(off));
     QB_CUDA(ctx, ctx->d_stats.ensure(2 * QB_MAX_CLASS));
+    QB_CUDA(ctx, ctx->d_primcount.ensure(QB_MAX_CLASS));
     QB_CUDA(ctx, cudaStreamSynchronize(s));
     ctx->pairs_valid = true;
     return QB_OK;
@@ -471,15 +511,16 @@ int qb_jk_device(qb_ctx* ctx, const double* dD, double* dJ, double* dK, double t
     qb_count_kernel<<<ctx->nclass, 1024, 0, s>>>(plan, ctx->d_pairs.p, ctx->d_Q.p, ctx->d_npref.p, ctx->d_dmax.p,
                                                   thr, ctx->d_offs.p, ctx->d_stats.p);
     QB_CUDA(ctx, cudaGetLastError());
+    QB_CUDA(ctx, cudaMemsetAsync(ctx->d_primcount.p, 0, QB_MAX_CLASS * sizeof(unsigned long long), s));
     QB_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
-    for (int k = 0; k < QB_NSTREAM; ++k) QB_CUDA(ctx, cudaStreamWaitEvent(ctx->streams[k], ctx->ev_fork, 0));
-    JKArgs args{ctx->d_prims.p, ctx->boys.p, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p, n};
+    for (int k2 = 0; k2 < QB_NSTREAM; ++k2) QB_CUDA(ctx, cudaStreamWaitEvent(ctx->streams[k2], ctx->ev_fork, 0));
     int k = 0;
     for (int c = ctx->nclass - 1; c >= 0; --c) {   // heavy classes first
         if (plan.nbra[c] == 0 || plan.nket[c] == 0) continue;
         ClassWork w{ctx->d_pairs.p + plan.bra_off[c], ctx->d_pairs.p + plan.ket_off[c],
                     ctx->d_offs.p + plan.offs_off[c], plan.nbra[c], plan.same[c]};
         const int grid = ctx->nsm * std::max(1, ctx->occ[c]);
+        JKArgs args{ctx->d_prims.p, ctx->boys.p, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p, ctx->d_primcount.p + c, n};
         ctx->launch[c].jk(w, args, grid, ctx->streams[k % QB_NSTREAM]);
         ++k;
     }

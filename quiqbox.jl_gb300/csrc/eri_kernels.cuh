@@ -23,6 +23,7 @@ struct JKArgs {
     const double* __restrict__ D;          // ratio-scaled density, column-major
     double* Jp;                            // J' accumulator (column-major nfun x nfun)
     double* Kp;                            // K' accumulator
+    unsigned long long* primcount;         // primitive quartets evaluated (this class)
     int nfun;
 };
 
@@ -54,6 +55,7 @@ __global__ void __launch_bounds__(128) qb_jk_class_kernel(const ClassWork w, con
     constexpr int NA = C::NA, NB = C::NB, NC = C::NC, ND = C::ND;
     const long long total = __ldg(w.offs + w.nbra);
     const long long stride = (long long)gridDim.x * blockDim.x;
+    unsigned nprimq = 0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
         const int i = qb_find_bra(w.offs, w.nbra, t);
         const int j = (int)(t - __ldg(w.offs + i));
@@ -61,7 +63,7 @@ __global__ void __launch_bounds__(128) qb_jk_class_kernel(const ClassWork w, con
         const ShellPair Q = w.ket[j];
         double I[C::NINT];
         C::block(a.prims + P.prim0, P.nprim, a.prims + Q.prim0, Q.nprim, P.ABx, P.ABy, P.ABz,
-                 Q.ABx, Q.ABy, Q.ABz, a.boys, I);
+                 Q.ABx, Q.ABy, Q.ABz, a.boys, I, nprimq);
         const double deg = (P.same ? 1.0 : 2.0) * (Q.same ? 1.0 : 2.0) * ((w.same && i == j) ? 1.0 : 2.0);
         const int N = a.nfun;
         const double* __restrict__ D = a.D;
@@ -145,6 +147,9 @@ __global__ void __launch_bounds__(128) qb_jk_class_kernel(const ClassWork w, con
 #pragma unroll
             for (int y = 0; y < ND; ++y) atomicAdd(Kp + (P.fb + x) + (size_t)N * (Q.fb + y), deg * Kbd[x * ND + y]);
     }
+    unsigned long long cnt = nprimq;
+    for (int d = 16; d > 0; d >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, d);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(a.primcount, cnt);
 }
 
 // Host-side launchers, one set per class (defined in the generated eri_class_*.cu).

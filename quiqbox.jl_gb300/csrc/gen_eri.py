@@ -317,12 +317,16 @@ class ClassGen:
         o.append("  static __device__ __forceinline__ void block(")
         o.append("      const PrimPair* __restrict__ bp, int nbp, const PrimPair* __restrict__ kp, int nkp,")
         o.append("      double ABx, double ABy, double ABz, double CDx, double CDy, double CDz,")
-        o.append("      const double* __restrict__ boys_tab, double (&I)[NINT]) {")
+        o.append("      const double* __restrict__ boys_tab, double (&I)[NINT], unsigned& nprimq) {")
         for e in self.esets:
             for f in self.fsets:
                 o.append(f"  double acc_{tname(e)}_{tname(f)} = 0.0;")
+        o.append("  // primitive pairs are sorted by descending |K|: stop once the prefactor bound")
+        o.append("  // |K_ab K_cd| drops below QB_PRIM_EPS")
+        o.append("  const double kmax_ket = nkp > 0 ? fabs(__ldg(&kp[0].K)) : 0.0;")
         o.append("  for (int ib = 0; ib < nbp; ++ib) {")
         o.append("    const PrimPair B = qb_load_pair(bp + ib);")
+        o.append("    if (fabs(B.K) * kmax_ket < QB_PRIM_EPS) break;")
         o.append("    const double p = B.p, Px = B.Px, Py = B.Py, Pz = B.Pz, Kab = B.K;")
         if la + lb > 0:
             o.append("    const double PAx = B.PAx, PAy = B.PAy, PAz = B.PAz;")
@@ -332,6 +336,8 @@ class ClassGen:
                 o.append(f"    const double oo2p_{k} = {float(k)} * oo2p;")
         o.append("    for (int ik = 0; ik < nkp; ++ik) {")
         o.append("      const PrimPair Kt = qb_load_pair(kp + ik);")
+        o.append("      if (fabs(B.K * Kt.K) < QB_PRIM_EPS) break;")
+        o.append("      ++nprimq;")
         o.append("      const double q = Kt.p, Qx = Kt.Px, Qy = Kt.Py, Qz = Kt.Pz, Kcd = Kt.K;")
         if lc + ld > 0:
             o.append("      const double QCx = Kt.PAx, QCy = Kt.PAy, QCz = Kt.PAz;")

@@ -19,6 +19,10 @@
 #define QB_BOYS_NM 41         // orders m = 0 .. 40
 #define QB_BOYS_NJ 8          // Taylor terms
 
+// Primitive quartets with |K_ab K_cd| below this bound are skipped by the class
+// kernels (the prefactor of every integral of the quartet is below 2.3 x this).
+#define QB_PRIM_EPS 1e-20
+
 // Largest total angular momentum of the generic (per-function) kernels.
 #define QB_GEN_LTOT_MAX 32
 

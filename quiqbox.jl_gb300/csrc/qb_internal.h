@@ -110,7 +110,8 @@ struct qb_ctx {
     int class_bra[QB_MAX_CLASS] = {}, class_ket[QB_MAX_CLASS] = {};
     long long offs_off[QB_MAX_CLASS + 1] = {};
     DevArray<long long> d_offs;
-    DevArray<long long> d_stats;          // 2 per class: quartets, primitive quartets
+    DevArray<long long> d_stats;          // 2 per class: quartets, primitive quartets (upper bound)
+    DevArray<unsigned long long> d_primcount;   // per class: primitive quartets evaluated
 
     // J/K buffers
     double schwarz = 1e-12;
