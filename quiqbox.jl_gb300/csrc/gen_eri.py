@@ -321,12 +321,16 @@ class ClassGen:
         for e in self.esets:
             for f in self.fsets:
                 o.append(f"  double acc_{tname(e)}_{tname(f)} = 0.0;")
-        o.append("  // primitive pairs are sorted by descending |K|: stop once the prefactor bound")
-        o.append("  // |K_ab K_cd| drops below QB_PRIM_EPS")
+        o.append("  // Primitive pairs are sorted by descending |K|.  One flattened loop walks the")
+        o.append("  // (bra, ket) primitive pairs with |K_ab K_cd| >= QB_PRIM_EPS, so that a warp runs")
+        o.append("  // max-over-lanes of the total count rather than of every inner loop.")
         o.append("  const double kmax_ket = nkp > 0 ? fabs(__ldg(&kp[0].K)) : 0.0;")
-        o.append("  for (int ib = 0; ib < nbp; ++ib) {")
-        o.append("    const PrimPair B = qb_load_pair(bp + ib);")
-        o.append("    if (fabs(B.K) * kmax_ket < QB_PRIM_EPS) break;")
+        o.append("  int ib = 0, ik = 0;")
+        o.append("  bool active = nbp > 0 && fabs(__ldg(&bp[0].K)) * kmax_ket >= QB_PRIM_EPS;")
+        o.append("  PrimPair B;")
+        o.append("  if (active) B = qb_load_pair(bp);")
+        o.append("  while (active) {")
+        o.append("    {")
         o.append("    const double p = B.p, Px = B.Px, Py = B.Py, Pz = B.Pz, Kab = B.K;")
         if la + lb > 0:
             o.append("    const double PAx = B.PAx, PAy = B.PAy, PAz = B.PAz;")
@@ -334,9 +338,7 @@ class ClassGen:
             o.append("    const double oo2p = B.oo2p;")
             for k in range(1, o2p + 1):
                 o.append(f"    const double oo2p_{k} = {float(k)} * oo2p;")
-        o.append("    for (int ik = 0; ik < nkp; ++ik) {")
         o.append("      const PrimPair Kt = qb_load_pair(kp + ik);")
-        o.append("      if (fabs(B.K * Kt.K) < QB_PRIM_EPS) break;")
         o.append("      ++nprimq;")
         o.append("      const double q = Kt.p, Qx = Kt.Px, Qy = Kt.Py, Qz = Kt.Pz, Kcd = Kt.K;")
         if lc + ld > 0:
@@ -347,6 +349,14 @@ class ClassGen:
         o += setup
         o += body
         o.append("      }")
+        o.append("    }")
+        o.append("    // advance to the next significant primitive quartet")
+        o.append("    ++ik;")
+        o.append("    if (ik >= nkp || fabs(B.K * __ldg(&kp[ik].K)) < QB_PRIM_EPS) {")
+        o.append("      ++ib;")
+        o.append("      ik = 0;")
+        o.append("      if (ib >= nbp || fabs(__ldg(&bp[ib].K)) * kmax_ket < QB_PRIM_EPS) active = false;")
+        o.append("      else B = qb_load_pair(bp + ib);")
         o.append("    }")
         o.append("  }")
         o += hrr
