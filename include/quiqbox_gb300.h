@@ -150,6 +150,26 @@ int qb_run_hartree_fock(qb_ctx* ctx, const qb_basis* basis, int nnuc, const doub
 /* Measured FP64 FMA throughput of this device (TFLOP/s), the FP64 roofline denominator. */
 int qb_fp64_peak(qb_ctx* ctx, double* tflops);
 
+/* Allocation-free direct J/K (no counterpart in the reference).
+ * For callers that cannot allocate device memory themselves (code inside a host
+ * framework that owns every device allocation, or code that must not allocate
+ * between graph captures): computes the same J and K as qb_jk with the generic
+ * per-function kernels and calls no cudaMalloc / cudaFree.  Everything is device
+ * memory owned by the caller: `dbasis` holds DEVICE pointers (fun_ptr, center, ijk,
+ * alpha, weight), dD is the nfun x nfun density, dJ / dK receive the results;
+ * `stream` is a cudaStream_t (NULL = legacy default stream).  No Schwarz screening.
+ *  - Limit: nfun <= 512; larger bases return QB_ERR_DIM before touching any pointer.
+ *  - Scratch: a file-scope device array of 4 MiB (+ a 1.7 MiB Boys table) held by
+ *    every GPU that loads the library until exit.  The first call on a device does
+ *    the set-up (resolves the arrays' device addresses, uploads the Boys table) and
+ *    must come before any stream capture on that device.
+ *  - Every call shares the array: calls that overlap on the GPU (other streams,
+ *    other host threads) race and corrupt each other's results.
+ *  - Bad basis data returns QB_ERR_ARG (pointer layout), QB_ERR_UNSUPPORTED
+ *    (angular momentum > 12) or QB_ERR_DOMAIN (exponent <= 0).  No context, so no
+ *    qb_last_error() message. */
+int qb_jk_noalloc(const qb_basis* dbasis, const double* dD, double* dJ, double* dK, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

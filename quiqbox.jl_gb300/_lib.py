@@ -20,7 +20,7 @@ QB_OK, QB_ERR_ARG, QB_ERR_DIM, QB_ERR_DOMAIN, QB_ERR_CUDA, QB_ERR_TIMEOUT, QB_ER
 EXPORTED = ["qb_create", "qb_destroy", "qb_last_error", "qb_device_info", "qb_overlaps", "qb_elec_kinetics",
             "qb_nuc_attractions", "qb_core_hamiltonian", "qb_elec_repulsions", "qb_elec_repulsion_list", "qb_jk",
             "qb_jk_prepare", "qb_jk_upload_density", "qb_jk_execute", "qb_jk_download", "qb_jk_get_stats", "qb_jk_pair_table",
-            "qb_scf_config_default", "qb_run_hartree_fock", "qb_fp64_peak"]
+            "qb_scf_config_default", "qb_run_hartree_fock", "qb_fp64_peak", "qb_jk_noalloc"]
 
 
 class DimensionMismatch(ValueError):
@@ -103,6 +103,7 @@ def load():
         L.qb_run_hartree_fock.argtypes = [vp, pb, C.c_int, pd, pd, C.c_int, C.c_int, C.POINTER(QBSCFConfig),
                                           C.POINTER(QBSCFResult)]
         L.qb_fp64_peak.argtypes = [vp, pd]
+        L.qb_jk_noalloc.argtypes = [pb, vp, vp, vp, vp]
         for name in EXPORTED:
             f = getattr(L, name)
             if name not in ("qb_destroy", "qb_last_error", "qb_scf_config_default"):
