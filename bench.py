@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--schwarz", type=float, default=1e-12)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--jk-only", type=int, default=0,
+                    help="profiling driver: prepare the workload, run this many J/K builds, print timings, exit")
     return ap.parse_args()
 
 
@@ -385,8 +387,30 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_jk_only(args):
+    """A fixed number of device-resident J/K builds of the bench workload (for ncu captures)."""
+    import __graft_entry__ as ge
+    qb = ge.load_package()
+    from quiqbox_gb300 import _lib as L
+    ctx = qb.Context(0)
+    fb, D = workload(qb, args.seed)
+    b = L.BasisArgs(fb)
+    Df = np.ascontiguousarray(D.reshape(-1, order="F"))
+    ctx.check(ctx.lib.qb_jk_prepare(ctx.h, b.ref(), args.schwarz))
+    ctx.check(ctx.lib.qb_jk_upload_density(ctx.h, L.dptr(Df)))
+    st = L.QBJKStats()
+    for _ in range(args.jk_only):
+        ctx.check(ctx.lib.qb_jk_execute(ctx.h))
+        ctx.check(ctx.lib.qb_jk_get_stats(ctx.h, C.byref(st)))
+        print(json.dumps({"ms": st.ms_last, "quartets": st.quartets, "prim_quartets": st.prim_quartets,
+                          "flops": st.flops}), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
+    if a.jk_only:
+        run_jk_only(a)
+        sys.exit(0)
     if a.warmup < 3:
         a.warmup = 3
     if a.impl == "reference":
