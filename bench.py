@@ -404,6 +404,9 @@ def run_jk_only(args):
         ctx.check(ctx.lib.qb_jk_get_stats(ctx.h, C.byref(st)))
         print(json.dumps({"ms": st.ms_last, "quartets": st.quartets, "prim_quartets": st.prim_quartets,
                           "flops": st.flops}), flush=True)
+    classes = {"".join(str(v) for v in st.class_l[c]): [st.class_quartets[c], st.class_prim_quartets[c]]
+               for c in range(st.nclass)}
+    print(json.dumps({"class_quartets_prim_quartets": classes}), flush=True)
 
 
 if __name__ == "__main__":

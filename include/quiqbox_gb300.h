@@ -67,6 +67,12 @@ int qb_nuc_attractions(qb_ctx* ctx, const qb_basis* basis, int nnuc, const doubl
 int qb_core_hamiltonian(qb_ctx* ctx, const qb_basis* basis, int nnuc, const double* Z, const double* R,
                         double* H);
 
+/* Boys function sequence on the device: F[i*(M+1) + m] = F_m(T[i]), m = 0..M, T[i] >= 0.
+ * Replaces computeBoysSequence (src/Integration/Engines/BoysFunction.jl:67-77) and
+ * computeBoysFunc (:62-64).  path 0: the evaluator of the ERI class kernels (M <= 8);
+ * path 1: the evaluator of the generic kernels (M <= 32). */
+int qb_boys(qb_ctx* ctx, int n, const double* T, int M, int path, double* F);
+
 /* Two-electron integrals (chemists' notation (ij|kl)).
  * qb_elec_repulsions <- src/Integration/Interface.jl:356 (elecRepulsions): nfun^4 tensor [i,j,k,l]
  * qb_elec_repulsion_list <- src/Integration/Interface.jl:331 (elecRepulsion) for nq explicit

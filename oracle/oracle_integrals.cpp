@@ -149,10 +149,16 @@ R direct_boys(R x, int n) {
 }
 
 // initializeUpperOrder (BoysFunction.jl:27-31)
+// At x = n = 1 the ratio is 1 and the formula diverges (the reference's Int(ceil(Inf))
+// raises InexactError there); its limit is taken, so that min(., 6n) picks 6n.
 template <class R>
 int upper_order(R x, int n) {
     const R ratio = ((R)n == x) ? (R)n : (R)n / x;
-    const int res = int(m_ceil((R)Tr<R>::digits / m_fabs(m_log10(ratio)) + n));
+    const R lg = m_fabs(m_log10(ratio));
+    if (!(lg > 0)) return 1 << 30;
+    const R up = m_ceil((R)Tr<R>::digits / lg + n);
+    if (up > (R)(1 << 30)) return 1 << 30;
+    const int res = int(up);
     return res + (res & 1);
 }
 

@@ -284,6 +284,25 @@ def runHartreeFock(nucInfo, basis, config: Optional[HFconfig] = None, spin=None,
                        res.steps, (na, nb))
 
 
+def computeBoysSequence(T, M, path=0, ctx=None):
+    """F_0..F_M at every T (array of shape T.shape + (M+1,)), evaluated on the device.
+
+    Mirrors computeBoysSequence (src/Integration/Engines/BoysFunction.jl:67-77).
+    path 0 is the evaluator of the ERI class kernels (M <= 8), path 1 that of the
+    generic kernels (M <= 32)."""
+    c = _ctx(ctx)
+    T = np.ascontiguousarray(np.asarray(T, dtype=np.float64))
+    flat = T.reshape(-1)
+    out = np.empty((flat.size, M + 1))
+    c.check(c.lib.qb_boys(c.h, C.c_int(flat.size), L.dptr(flat), C.c_int(M), C.c_int(path), L.dptr(out)))
+    return out.reshape(T.shape + (M + 1,))
+
+
+def computeBoysFunc(T, m, ctx=None):
+    """F_m(T) on the device (computeBoysFunc, src/Integration/Engines/BoysFunction.jl:62-64)."""
+    return float(computeBoysSequence(np.array([T]), m, path=1 if m > 8 else 0, ctx=ctx)[0, m])
+
+
 def fp64_peak(ctx=None):
     """Measured FP64 FMA throughput of the device (TFLOP/s)."""
     c = _ctx(ctx)

@@ -1,5 +1,6 @@
 // C ABI entry points (include/quiqbox_gb300.h).
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -55,7 +56,21 @@ int qb_create(qb_ctx** out, int device) {
     if (rc == QB_OK) {
         ctx->nclass = QB_NCLASS;
         qb_get_class_launchers(ctx->launch);
-        for (int c = 0; c < ctx->nclass; ++c) ctx->occ[c] = ctx->launch[c].occupancy();
+        // Variant per class: the generator's measured preference.  QB_JK_VARIANT overrides
+        // it for tuning: "thread", "warp", or one character per class ('t'/'w').
+        const char* ov = getenv("QB_JK_VARIANT");
+        for (int c = 0; c < ctx->nclass; ++c) {
+            const ClassLaunchers& L = ctx->launch[c];
+            int v = (L.preferred && L.jk[1]) ? 1 : 0;
+            if (ov) {
+                if (!strcmp(ov, "thread")) v = 0;
+                else if (strlen(ov) == (size_t)ctx->nclass) v = (ov[c] == 'w') ? 1 : 0;
+                v = (v && L.jk[1]) ? 1 : 0;
+                if (!strcmp(ov, "warp")) v = L.jk[1] ? 1 : 0;
+            }
+            ctx->variant[c] = v;
+            ctx->occ[c] = L.occupancy[v]();
+        }
         rc = qb_cuda_check(ctx, cudaGetLastError(), "kernel occupancy query");
     }
     if (rc != QB_OK) {
@@ -160,6 +175,25 @@ int qb_elec_repulsion_list(qb_ctx* ctx, const qb_basis* basis, int64_t nq, const
     QB_CUDA(ctx, cudaMemcpyAsync(out, ctx->d_big.p, nq * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     QB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return qb_check_status(ctx);
+}
+
+int qb_boys(qb_ctx* ctx, int n, const double* T, int M, int path, double* F) {
+    QB_TRY(enter(ctx));
+    if (n < 0 || (n > 0 && (!T || !F))) return qb_set_error(ctx, QB_ERR_ARG, "bad Boys arguments");
+    if (path != 0 && path != 1) return qb_set_error(ctx, QB_ERR_ARG, "Boys path must be 0 or 1");
+    if (M < 0 || M > (path == 0 ? 8 : QB_GEN_LTOT_MAX)) return qb_set_error(ctx, QB_ERR_DIM, "Boys order out of range");
+    for (int i = 0; i < n; ++i)
+        if (!(T[i] >= 0.0) || !std::isfinite(T[i])) return qb_set_error(ctx, QB_ERR_DOMAIN, "Boys argument must be finite and >= 0");
+    if (n == 0) return QB_OK;
+    QB_CUDA(ctx, ctx->d_m0.ensure((size_t)n));
+    QB_CUDA(ctx, ctx->d_big.ensure((size_t)n * (M + 1)));
+    QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_m0.p, T, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    if (qb_boys_device(n, ctx->d_m0.p, M, path, ctx->boys.p, ctx->d_big.p, ctx->stream) != 0)
+        return qb_cuda_check(ctx, cudaGetLastError(), "Boys kernel");
+    QB_CUDA(ctx, cudaMemcpyAsync(F, ctx->d_big.p, (size_t)n * (M + 1) * sizeof(double), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    QB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return QB_OK;
 }
 
 int qb_jk_prepare(qb_ctx* ctx, const qb_basis* basis, double schwarz) {

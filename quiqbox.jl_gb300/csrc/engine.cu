@@ -30,12 +30,12 @@ int qb_cuda_check(qb_ctx* ctx, cudaError_t e, const char* where) {
 // ---------------------------------------------------------------------------
 // Boys table: F_m(T_k), T_k = k/16, by the power series
 //   F_m(T) = e^{-T} sum_i (2T)^i / ((2m+1)(2m+3)...(2m+2i+1))
-// in extended precision, then stored as the Taylor coefficients of qb_common.cuh.
-std::vector<double> qb_build_boys_table() {
+// in extended precision, then stored as the Taylor coefficients of qb_common.cuh,
+// followed by e^{-T_k}.  Writes QB_BOYS_TABLE_SIZE doubles; allocates nothing.
+void qb_fill_boys_table(double* tab) {
     const int NM = QB_BOYS_NM, NJ = QB_BOYS_NJ, MT = NM + NJ - 1;
-    std::vector<double> tab((size_t)QB_BOYS_NROW * NM * NJ);
-    std::vector<long double> F(MT + 1);
-    long double fact[NJ];
+    long double F[QB_BOYS_NM + QB_BOYS_NJ];
+    long double fact[QB_BOYS_NJ];
     fact[0] = 1.0L;
     for (int j = 1; j < NJ; ++j) fact[j] = fact[j - 1] * j;
     for (int k = 0; k < QB_BOYS_NROW; ++k) {
@@ -55,7 +55,13 @@ std::vector<double> qb_build_boys_table() {
                 const long double c = F[m + j] / fact[j] * ((j & 1) ? -1.0L : 1.0L);
                 tab[((size_t)k * NM + m) * NJ + j] = (double)c;
             }
+        tab[QB_BOYS_EXP_OFF + k] = (double)ex;
     }
+}
+
+std::vector<double> qb_build_boys_table() {
+    std::vector<double> tab(QB_BOYS_TABLE_SIZE);
+    qb_fill_boys_table(tab.data());
     return tab;
 }
 
@@ -229,7 +235,9 @@ __global__ void qb_primpair_kernel(const PairSlot* __restrict__ slots, int n, co
     const double c0 = 5.9149671727956128778;
     r.K = c0 * w[s.pa] * w[s.pb] * exp(-a * b * ip * ab2) * ip;
     r.oo2p = 0.5 * ip;
-    r.pad = 0.0;
+    float* kf = reinterpret_cast<float*>(&r.pad);
+    kf[0] = (float)fabs(r.K);
+    kf[1] = 0.0f;
     out[k] = r;
     atomicMax(kmax, (unsigned long long)__double_as_longlong(fabs(r.K)));
 }
@@ -521,7 +529,7 @@ int qb_jk_device(qb_ctx* ctx, const double* dD, double* dJ, double* dK, double t
                     ctx->d_offs.p + plan.offs_off[c], plan.nbra[c], plan.same[c]};
         const int grid = ctx->nsm * std::max(1, ctx->occ[c]);
         JKArgs args{ctx->d_prims.p, ctx->boys.p, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p, ctx->d_primcount.p + c, n};
-        ctx->launch[c].jk(w, args, grid, ctx->streams[k % QB_NSTREAM]);
+        ctx->launch[c].jk[ctx->variant[c]](w, args, grid, ctx->streams[k % QB_NSTREAM]);
         ++k;
     }
     QB_CUDA(ctx, cudaGetLastError());

@@ -132,7 +132,35 @@ class ClassGen:
             need.add(n)
             stack.extend(self.vrr_children(n))
         order = sorted(need, key=lambda n: (sum(n[0]) + sum(n[1]), sum(n[1]), -n[2], n))
-        return order, targets
+        return self.schedule(order), targets
+
+    def schedule(self, nodes):
+        """Emission order of the VRR nodes: greedy list scheduling that, among the nodes whose
+        inputs are ready, takes the one that frees the most live values (ties: lower angular
+        momentum first).  Keeps the live set ~35% below a level-by-level order, which is
+        what decides register spilling in the larger classes."""
+        ch = {n: sorted(set(self.vrr_children(n))) for n in nodes}
+        parents = {n: [] for n in nodes}
+        for n in nodes:
+            for c in ch[n]:
+                parents[c].append(n)
+        uses = {n: len(parents[n]) for n in nodes}
+        ndeps = {n: len(ch[n]) for n in nodes}
+        ready = [n for n in nodes if ndeps[n] == 0]
+        out = []
+        while ready:
+            best = min(ready, key=lambda n: ((1 if parents[n] else 0) - sum(1 for c in ch[n] if uses[c] == 1),
+                                             sum(n[0]) + sum(n[1]), n))
+            ready.remove(best)
+            out.append(best)
+            for c in ch[best]:
+                uses[c] -= 1
+            for par in parents[best]:
+                ndeps[par] -= 1
+                if ndeps[par] == 0:
+                    ready.append(par)
+        assert len(out) == len(nodes)
+        return out
 
     @staticmethod
     def vname(n):
@@ -143,6 +171,7 @@ class ClassGen:
 
     def emit_vrr(self, out, ind):
         order, targets = self.vrr_nodes()
+        tindex = {t: k for k, t in enumerate(targets)}
         c = self.prim
         for n in order:
             e, f, m = n
@@ -180,9 +209,12 @@ class ClassGen:
                     expr = f"fma(oo2p_{e1[i]}, fma(-qpq, {b1}, {b0}), {expr})"
                     c.fma += 2
             out.append(f"{ind}const double {nm} = {expr};")
-        for t in targets:
-            out.append(f"{ind}acc_{tname(t[0])}_{tname(t[1])} += {self.vname(t)};")
-            c.add += 1
+            if n in tindex:
+                out.append(f"{ind}sink({tindex[n]}, {nm});")
+        for k, t in enumerate(targets):
+            if sum(t[0]) == 0 and sum(t[1]) == 0:
+                out.append(f"{ind}sink({k}, {self.vname(t)});")
+        c.add += len(targets)   # the accumulation of every target into its contracted sum
         used_m = sorted({n[2] for n in order if sum(n[0]) == 0 and sum(n[1]) == 0})
         maxo2p = max([n[0][pick_axis(n[0])] - 1 for n in order if sum(n[1]) == 0 and sum(n[0]) > 0] + [0])
         maxo2q = max([n[1][pick_axis(n[1])] - 1 for n in order if sum(n[1]) > 0] + [0])
@@ -287,50 +319,39 @@ class ClassGen:
         L(f"{ind}qb_boys_scaled<{M}>(T, pre, boys_tab, F);")
         for m in used_m:
             L(f"{ind}const double F{m} = F[{m}];")
-        # Boys cost as emitted by qb_boys_scaled (qb_common.cuh): Taylor on the
-        # Horner form (7 fma), the prefactor scaling and, for M>2, exp(-T)
-        # (counted as 12 flops) plus the downward recursion (fma+mul per order).
+        # Boys cost as emitted by qb_boys_scaled (qb_common.cuh), table branch: Taylor on
+        # the Horner form (7 fma per order evaluated) and the prefactor scaling; for M > 2
+        # one Horner evaluation, e^{-T} from the table (degree-8 Taylor, 2 mul) and the
+        # downward recursion (fma + mul per order).
         if M <= 2:
             c.fma += 7 * (M + 1)
             c.mul += M + 1
         else:
-            c.fma += 7 + M
-            c.mul += 2 + 1 + M
-            c.add += 12
+            c.fma += 7 + 8 + M
+            c.mul += 1 + 2 + M
 
     def generate(self):
         la, lb, lc, ld = self.la, self.lb, self.lc, self.ld
         na, nb, nc, nd = ncart(la), ncart(lb), ncart(lc), ncart(ld)
         nint = na * nb * nc * nd
+        nt = len(self.esets) * len(self.fsets)
         body = []
-        ind = "      "
-        used_m, o2p, o2q, o2pq = self.emit_vrr(body, ind + "  ")
+        ind = "    "
+        used_m, o2p, o2q, o2pq = self.emit_vrr(body, ind)
         setup = []
-        self.emit_quartet_setup(setup, ind + "  ", used_m, o2q, o2pq)
+        self.emit_quartet_setup(setup, ind, used_m, o2q, o2pq)
         hrr = []
-        self.emit_hrr(hrr, "  ")
+        self.emit_hrr(hrr, "    ")
         o = []
         o.append(f"// class ({la}{lb}|{lc}{ld}): {len(self.esets)}x{len(self.fsets)} contracted "
                  f"[e0|f0], {nint} integrals")
         o.append(f"template <> struct EriClass<{la}, {lb}, {lc}, {ld}> {{")
-        o.append(f"  static constexpr int NA = {na}, NB = {nb}, NC = {nc}, ND = {nd}, NINT = {nint};")
-        o.append("  static __device__ __forceinline__ void block(")
-        o.append("      const PrimPair* __restrict__ bp, int nbp, const PrimPair* __restrict__ kp, int nkp,")
-        o.append("      double ABx, double ABy, double ABz, double CDx, double CDy, double CDz,")
-        o.append("      const double* __restrict__ boys_tab, double (&I)[NINT], unsigned& nprimq) {")
-        for e in self.esets:
-            for f in self.fsets:
-                o.append(f"  double acc_{tname(e)}_{tname(f)} = 0.0;")
-        o.append("  // Primitive pairs are sorted by descending |K|.  One flattened loop walks the")
-        o.append("  // (bra, ket) primitive pairs with |K_ab K_cd| >= QB_PRIM_EPS, so that a warp runs")
-        o.append("  // max-over-lanes of the total count rather than of every inner loop.")
-        o.append("  const double kmax_ket = nkp > 0 ? fabs(__ldg(&kp[0].K)) : 0.0;")
-        o.append("  int ib = 0, ik = 0;")
-        o.append("  bool active = nbp > 0 && fabs(__ldg(&bp[0].K)) * kmax_ket >= QB_PRIM_EPS;")
-        o.append("  PrimPair B;")
-        o.append("  if (active) B = qb_load_pair(bp);")
-        o.append("  while (active) {")
-        o.append("    {")
+        o.append(f"  static constexpr int NA = {na}, NB = {nb}, NC = {nc}, ND = {nd}, NINT = {nint}, NT = {nt};")
+        o.append("  // VRR targets [e0|f0]^(0) of one primitive quartet (bra pair B, ket pair Kt), prefactor")
+        o.append("  // included: sink(k, value) receives target k (in (e, f) order) as soon as it is final.")
+        o.append("  template <class Sink>")
+        o.append("  static __device__ __forceinline__ void prim(const PrimPair& B, const PrimPair& Kt,")
+        o.append("                                              const double* __restrict__ boys_tab, Sink&& sink) {")
         o.append("    const double p = B.p, Px = B.Px, Py = B.Py, Pz = B.Pz, Kab = B.K;")
         if la + lb > 0:
             o.append("    const double PAx = B.PAx, PAy = B.PAy, PAz = B.PAz;")
@@ -338,32 +359,72 @@ class ClassGen:
             o.append("    const double oo2p = B.oo2p;")
             for k in range(1, o2p + 1):
                 o.append(f"    const double oo2p_{k} = {float(k)} * oo2p;")
-        o.append("      const PrimPair Kt = qb_load_pair(kp + ik);")
-        o.append("      ++nprimq;")
-        o.append("      const double q = Kt.p, Qx = Kt.Px, Qy = Kt.Py, Qz = Kt.Pz, Kcd = Kt.K;")
+        o.append("    const double q = Kt.p, Qx = Kt.Px, Qy = Kt.Py, Qz = Kt.Pz, Kcd = Kt.K;")
         if lc + ld > 0:
-            o.append("      const double QCx = Kt.PAx, QCy = Kt.PAy, QCz = Kt.PAz;")
+            o.append("    const double QCx = Kt.PAx, QCy = Kt.PAy, QCz = Kt.PAz;")
         if o2q:
-            o.append("      const double oo2q = Kt.oo2p;")
-        o.append("      {")
+            o.append("    const double oo2q = Kt.oo2p;")
         o += setup
         o += body
-        o.append("      }")
-        o.append("    }")
-        o.append("    // advance to the next significant primitive quartet")
-        o.append("    ++ik;")
-        o.append("    if (ik >= nkp || fabs(B.K * __ldg(&kp[ik].K)) < QB_PRIM_EPS) {")
-        o.append("      ++ib;")
-        o.append("      ik = 0;")
-        o.append("      if (ib >= nbp || fabs(__ldg(&bp[ib].K)) * kmax_ket < QB_PRIM_EPS) active = false;")
-        o.append("      else B = qb_load_pair(bp + ib);")
-        o.append("    }")
         o.append("  }")
+        o.append("  // Contracted targets -> (ab|cd) block by the horizontal recursion.")
+        o.append("  // A[k] is the contracted target k: a register array or a shared-memory row.")
+        o.append("  template <class Acc>")
+        o.append("  static __device__ __forceinline__ void hrr(const Acc& A, double ABx, double ABy, double ABz,")
+        o.append("                                             double CDx, double CDy, double CDz, double (&I)[NINT]) {")
+        k = 0
+        for e in self.esets:
+            for f in self.fsets:
+                o.append(f"    const double acc_{tname(e)}_{tname(f)} = A[{k}];")
+                k += 1
         o += hrr
         o.append("  }")
+        o.append("  // One contracted quartet in one thread: a flattened loop over the primitive quartets")
+        o.append("  // with |K_ab K_cd| >= QB_PRIM_EPS (pairs sorted by descending |K|), then the HRR.")
+        o.append("  static __device__ __forceinline__ void block(")
+        o.append("      const PrimPair* __restrict__ bp, int nbp, const PrimPair* __restrict__ kp, int nkp,")
+        o.append("      double ABx, double ABy, double ABz, double CDx, double CDy, double CDz,")
+        o.append("      const double* __restrict__ boys_tab, double (&I)[NINT], unsigned& nprimq) {")
+        o.append("    double A[NT];")
+        o.append("#pragma unroll")
+        o.append("    for (int t = 0; t < NT; ++t) A[t] = 0.0;")
+        o.append("    const double kmax_ket = nkp > 0 ? fabs(__ldg(&kp[0].K)) : 0.0;")
+        o.append("    int ib = 0, ik = 0;")
+        o.append("    bool active = nbp > 0 && fabs(__ldg(&bp[0].K)) * kmax_ket >= QB_PRIM_EPS;")
+        o.append("    PrimPair B;")
+        o.append("    if (active) B = qb_load_pair(bp);")
+        o.append("    while (active) {")
+        o.append("      const PrimPair Kt = qb_load_pair(kp + ik);")
+        o.append("      ++nprimq;")
+        o.append("      prim(B, Kt, boys_tab, [&](int t, double v) { A[t] += v; });")
+        o.append("      ++ik;")
+        o.append("      if (ik >= nkp || fabs(B.K * __ldg(&kp[ik].K)) < QB_PRIM_EPS) {")
+        o.append("        ++ib;")
+        o.append("        ik = 0;")
+        o.append("        if (ib >= nbp || fabs(__ldg(&bp[ib].K)) * kmax_ket < QB_PRIM_EPS) active = false;")
+        o.append("        else B = qb_load_pair(bp + ib);")
+        o.append("      }")
+        o.append("    }")
+        o.append("    hrr(A, ABx, ABy, ABz, CDx, CDy, CDz, I);")
+        o.append("  }")
         o.append("};")
-        # the bra oo2p multiples are per bra primitive pair: amortised over the ket loop
         return "\n".join(o)
+
+
+# Warp-cooperative kernel: 4 warps per block, one block per SM; each warp holds the
+# accumulator rows ((NT | 1) doubles) of G owner quartets in shared memory, G <= 32,
+# within 50 KiB per warp (the rest of the 227 KiB is the kernel's static tables).
+WARPS_PER_BLOCK = 4
+SMEM_PER_WARP = 50 * 1024
+
+
+# Classes whose per-thread kernel measured faster on GB300 than the warp-cooperative one
+# (J/K build of 64 H + 16 C/N/O, 3-primitive s/p/d shells): launched per thread by default.
+PREFER_PER_THREAD = {"2121", "2211", "2221"}
+
+
+def owners_per_warp(nt):
+    return max(0, min(32, SMEM_PER_WARP // ((nt | 1) * 8)))
 
 
 HEADER = """// GENERATED by gen_eri.py -- do not edit.
@@ -383,11 +444,20 @@ def main(outdir, lmax=LMAX_DEFAULT):
         name = g.name
         (outdir / f"eri_class_{name}.cuh").write_text(HEADER + code + "\n")
         la, lb, lc, ld = cls
+        nt = len(g.esets) * len(g.fsets)
+        g_own = owners_per_warp(nt)
+        wpb = WARPS_PER_BLOCK if g_own else 0
         cu = [f'// GENERATED by gen_eri.py -- do not edit.',
               f'#include "eri_class_{name}.cuh"', '#include "eri_kernels.cuh"',
-              f'QB_DEFINE_LAUNCHERS({la}, {lb}, {lc}, {ld})',
-              f"ClassLaunchers qb_class_{name}() {{ return {{qb_jk_launch_{name}, qb_occ_{name}, "
-              f"{la}, {lb}, {lc}, {ld}}}; }}"]
+              f'QB_DEFINE_LAUNCHERS({la}, {lb}, {lc}, {ld})']
+        if wpb:
+            cu.append(f'QB_DEFINE_WARP_LAUNCHERS({la}, {lb}, {lc}, {ld}, {wpb}, {g_own})')
+            wj, wo = f'qb_jkw_launch_{name}', f'qb_occw_{name}'
+        else:
+            wj, wo = 'nullptr', 'nullptr'
+        pref = 1 if (wpb and name not in PREFER_PER_THREAD) else 0
+        cu.append(f"ClassLaunchers qb_class_{name}() {{ return {{{{qb_jk_launch_{name}, {wj}}}, "
+                  f"{{qb_occ_{name}, {wo}}}, {la}, {lb}, {lc}, {ld}, {wpb}, {pref}}}; }}")
         (outdir / f"eri_class_{name}.cu").write_text("\n".join(cu) + "\n")
         files.append(name)
         table[name] = {"prim_flops": g.prim.flops(), "contr_flops": g.contr.flops(),

@@ -359,3 +359,44 @@ int qb_gen_schwarz(const GenDevBasis& gb, const double* boys, const ShellPair* p
     if (n > 0) qb_schwarz_generic_kernel<<<(n + 63) / 64, 64, 0, s>>>(b, boys, pairs, n, na, nb, Q, status);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
+
+// ---------------------------------------------------------------------------
+// Boys sequences F_0..F_M(T_i) by the device evaluators: path 0 the compile-time-order
+// version of the class kernels (M <= 8), path 1 the runtime-order version of the
+// generic kernels (M <= QB_GEN_LTOT_MAX).
+template <int M>
+__device__ void qb_boys_one(double T, const double* tab, double* out) {
+    double F[M + 1];
+    qb_boys_scaled<M>(T, 1.0, tab, F);
+#pragma unroll
+    for (int m = 0; m <= M; ++m) out[m] = F[m];
+}
+
+__global__ void qb_boys_kernel(int n, const double* __restrict__ T, int M, int path, const double* __restrict__ tab,
+                               double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double* o = out + (size_t)i * (M + 1);
+    if (path == 1) {
+        double F[QB_GEN_LTOT_MAX + 1];
+        qb_boys_scaled_rt(T[i], 1.0, tab, M, F);
+        for (int m = 0; m <= M; ++m) o[m] = F[m];
+        return;
+    }
+    switch (M) {
+        case 0: qb_boys_one<0>(T[i], tab, o); break;
+        case 1: qb_boys_one<1>(T[i], tab, o); break;
+        case 2: qb_boys_one<2>(T[i], tab, o); break;
+        case 3: qb_boys_one<3>(T[i], tab, o); break;
+        case 4: qb_boys_one<4>(T[i], tab, o); break;
+        case 5: qb_boys_one<5>(T[i], tab, o); break;
+        case 6: qb_boys_one<6>(T[i], tab, o); break;
+        case 7: qb_boys_one<7>(T[i], tab, o); break;
+        default: qb_boys_one<8>(T[i], tab, o); break;
+    }
+}
+
+int qb_boys_device(int n, const double* dT, int M, int path, const double* boys, double* dout, cudaStream_t s) {
+    if (n > 0) qb_boys_kernel<<<(n + 127) / 128, 128, 0, s>>>(n, dT, M, path, boys, dout);
+    return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}

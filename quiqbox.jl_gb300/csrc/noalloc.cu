@@ -18,35 +18,9 @@
 
 // J' (N^2) + K' (N^2) + status (one int, in its own 256-byte slot)
 static __device__ __align__(256) double qb_noalloc_scratch[2 * QB_NOALLOC_MAXN * QB_NOALLOC_MAXN + 32];
-static __device__ __align__(256) double qb_noalloc_boys[QB_BOYS_NROW * QB_BOYS_NM * QB_BOYS_NJ];
+static __device__ __align__(256) double qb_noalloc_boys[QB_BOYS_TABLE_SIZE];
 
 namespace {
-
-// Boys table of qb_common.cuh (F_m(T_k) by the power series in extended precision,
-// downward recursion, stored as Taylor coefficients), written into a caller buffer
-// without any heap allocation.
-void fill_boys_table(double* tab) {
-    const int NM = QB_BOYS_NM, NJ = QB_BOYS_NJ, MT = NM + NJ - 1;
-    long double F[QB_BOYS_NM + QB_BOYS_NJ];
-    long double fact[QB_BOYS_NJ];
-    fact[0] = 1.0L;
-    for (int j = 1; j < NJ; ++j) fact[j] = fact[j - 1] * j;
-    for (int k = 0; k < QB_BOYS_NROW; ++k) {
-        const long double T = (long double)k / 16.0L;
-        long double term = 1.0L / (2 * MT + 1), sum = term;
-        for (int i = 1; i < 100000; ++i) {
-            term *= 2.0L * T / (2 * MT + 2 * i + 1);
-            sum += term;
-            if (term < sum * 1e-30L) break;
-        }
-        const long double ex = expl(-T);
-        F[MT] = ex * sum;
-        for (int m = MT; m > 0; --m) F[m - 1] = (2.0L * T * F[m] + ex) / (2 * m - 1);
-        for (int m = 0; m < NM; ++m)
-            for (int j = 0; j < NJ; ++j)
-                tab[((size_t)k * NM + m) * NJ + j] = (double)(F[m + j] / fact[j] * ((j & 1) ? -1.0L : 1.0L));
-    }
-}
 
 struct NoAllocDevice {
     bool ready = false;
@@ -58,7 +32,7 @@ struct NoAllocDevice {
 constexpr int kMaxDevices = 64;
 NoAllocDevice g_dev[kMaxDevices];
 std::mutex g_mutex;
-double g_boys_host[QB_BOYS_NROW * QB_BOYS_NM * QB_BOYS_NJ];   // static staging, no heap
+double g_boys_host[QB_BOYS_TABLE_SIZE];   // static staging, no heap
 
 // Bad basis data set status bits instead of reaching the integral kernels.  The
 // function pointers are checked first (their last entry bounds the primitive arrays);
@@ -91,7 +65,7 @@ int setup_device(int dev) {
     if (d.ready) return QB_OK;
     static bool table_built = false;
     if (!table_built) {
-        fill_boys_table(g_boys_host);
+        qb_fill_boys_table(g_boys_host);
         table_built = true;
     }
     void* p = nullptr;

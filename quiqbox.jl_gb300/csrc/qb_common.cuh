@@ -9,15 +9,22 @@
 // ---------------------------------------------------------------------------
 // Boys function table.  Row k holds, for T_k = k/16 and every order m, the 8
 // Taylor coefficients c_j = F_{m+j}(T_k) (-1)^j / j!, so that
-//   F_m(T_k + d) = sum_j c_j d^j,  |d| <= 1/32   (relative error < 3e-17).
-// Above T = QB_BOYS_TMAX the asymptotic F_0 = sqrt(pi/T)/2 (erfc(sqrt 40) ~ 1e-19)
-// and the upward recursion F_{m+1} = ((2m+1) F_m - e^{-T}) / (2T) are used.
+//   F_m(T_k + d) = sum_j c_j d^j,  |d| <= 1/32   (relative error < 3e-17);
+// after the rows, e^{-T_k} for every k (e^{-T} = e^{-T_k} e^{-d} with a degree-8
+// Taylor polynomial of e^{-d}).
+// Above T = QB_BOYS_TMAX the asymptotic F_0 = sqrt(pi/T)/2 (erfc(sqrt 50) ~ 2e-24)
+// and the upward recursion F_{m+1} = ((2m+1) F_m - e^{-T}) / (2T) are used; for the
+// orders m <= QB_BOYS_ASYM_NOEXP_M the e^{-T} term is dropped: its share of F_m is
+// e^{-T} / (2T F_m) < 2e-15 for T >= 50.
 #define QB_BOYS_DT_INV 16.0
 #define QB_BOYS_DT 0.0625
-#define QB_BOYS_TMAX 40.0
-#define QB_BOYS_NROW 641      // T_k = 0 .. 40
+#define QB_BOYS_TMAX 50.0
+#define QB_BOYS_NROW 801      // T_k = 0 .. 50
 #define QB_BOYS_NM 41         // orders m = 0 .. 40
 #define QB_BOYS_NJ 8          // Taylor terms
+#define QB_BOYS_EXP_OFF (QB_BOYS_NROW * QB_BOYS_NM * QB_BOYS_NJ)
+#define QB_BOYS_TABLE_SIZE (QB_BOYS_EXP_OFF + QB_BOYS_NROW)
+#define QB_BOYS_ASYM_NOEXP_M 6
 
 // Primitive quartets with |K_ab K_cd| below this bound are skipped by the class
 // kernels (the prefactor of every integral of the quartet is below 2.3 x this).
@@ -41,6 +48,18 @@ __device__ __forceinline__ double qb_horner8(const double* __restrict__ c, doubl
     return r;
 }
 
+// e^{-d} for |d| <= 1/32: Taylor polynomial of degree 8 (truncation < 8e-20).
+__device__ __forceinline__ double qb_exp_neg_small(double d) {
+    double r = fma(d, 1.0 / 40320.0, -1.0 / 5040.0);
+    r = fma(r, d, 1.0 / 720.0);
+    r = fma(r, d, -1.0 / 120.0);
+    r = fma(r, d, 1.0 / 24.0);
+    r = fma(r, d, -1.0 / 6.0);
+    r = fma(r, d, 0.5);
+    r = fma(r, d, -1.0);
+    return fma(r, d, 1.0);
+}
+
 // F[m] = pre * F_m(T) for m = 0..M (compile-time M).
 template <int M>
 __device__ __forceinline__ void qb_boys_scaled(double T, double pre, const double* __restrict__ tab,
@@ -54,7 +73,7 @@ __device__ __forceinline__ void qb_boys_scaled(double T, double pre, const doubl
             for (int m = 0; m <= M; ++m) F[m] = pre * qb_horner8(row + m * QB_BOYS_NJ, d);
         } else {
             double f = pre * qb_horner8(row + M * QB_BOYS_NJ, d);
-            const double e = pre * exp(-T);
+            const double e = (pre * __ldg(tab + QB_BOYS_EXP_OFF + k)) * qb_exp_neg_small(d);
             const double T2 = T + T;
             F[M] = f;
 #pragma unroll
@@ -68,12 +87,20 @@ __device__ __forceinline__ void qb_boys_scaled(double T, double pre, const doubl
         double f = pre * QB_SQRT_PI_HALF * ir;
         F[0] = f;
         if (M > 0) {
-            const double e = pre * exp(-T);
             const double i2T = 0.5 * ir * ir;
+            if (M <= QB_BOYS_ASYM_NOEXP_M) {
 #pragma unroll
-            for (int m = 0; m < M; ++m) {
-                f = fma((double)(2 * m + 1), f, -e) * i2T;
-                F[m + 1] = f;
+                for (int m = 0; m < M; ++m) {
+                    f = f * ((double)(2 * m + 1) * i2T);
+                    F[m + 1] = f;
+                }
+            } else {
+                const double e = pre * exp(-T);
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    f = fma((double)(2 * m + 1), f, -e) * i2T;
+                    F[m + 1] = f;
+                }
             }
         }
     }
@@ -89,7 +116,7 @@ __device__ __forceinline__ void qb_boys_scaled_rt(double T, double pre, const do
         double f = pre * qb_horner8(row + M * QB_BOYS_NJ, d);
         F[M] = f;
         if (M > 0) {
-            const double e = pre * exp(-T);
+            const double e = (pre * __ldg(tab + QB_BOYS_EXP_OFF + k)) * qb_exp_neg_small(d);
             const double T2 = T + T;
             for (int m = M - 1; m >= 0; --m) {
                 f = fma(T2, f, e) / (double)(2 * m + 1);
@@ -101,7 +128,7 @@ __device__ __forceinline__ void qb_boys_scaled_rt(double T, double pre, const do
         double f = pre * QB_SQRT_PI_HALF * ir;
         F[0] = f;
         if (M > 0) {
-            const double e = pre * exp(-T);
+            const double e = (M <= QB_BOYS_ASYM_NOEXP_M) ? 0.0 : pre * exp(-T);
             const double i2T = 0.5 * ir * ir;
             for (int m = 0; m < M; ++m) {
                 f = fma((double)(2 * m + 1), f, -e) * i2T;
@@ -128,6 +155,12 @@ __device__ __forceinline__ PrimPair qb_load_pair(const PrimPair* __restrict__ pt
     r.p = a.x; r.Px = a.y; r.Py = b.x; r.Pz = b.y; r.PAx = c.x; r.PAy = c.y; r.PAz = d.x; r.K = d.y;
     r.oo2p = e.x; r.pad = e.y;
     return r;
+}
+
+// |K| of a primitive pair as a float, kept in the pad word (screening decisions in
+// the FP32 pipe).
+__device__ __forceinline__ float qb_kabs(const PrimPair* __restrict__ p) {
+    return __ldg(reinterpret_cast<const float*>(&p->pad));
 }
 
 // Shell pair (A, B) of a class list.

@@ -26,6 +26,7 @@ int qb_gen_onebody(const GenDevBasis& gb, int flags, int nnuc, const double* dZ,
                    const double* boys, double* S, double* T, double* V, int* status, cudaStream_t s);
 int qb_gen_eri(const GenDevBasis& gb, int mode, const double* boys, double* eri, const double* D, double* Jp,
                double* Kp, int* status, int nsm, cudaStream_t s);
+int qb_boys_device(int n, const double* dT, int M, int path, const double* boys, double* dout, cudaStream_t s);
 int qb_gen_schwarz(const GenDevBasis& gb, const double* boys, const ShellPair* pairs, int n, int na, int nb,
                    double* Q, int* status, cudaStream_t s);
 int qb_gen_eri_list(const GenDevBasis& gb, const double* boys, long long nq, const int* dq, double* out,
@@ -38,6 +39,7 @@ extern const double QB_CLASS_PRIM_FLOPS[];
 extern const double QB_CLASS_CONTR_FLOPS[];
 extern const int QB_CLASS_NINT[];
 void qb_get_class_launchers(ClassLaunchers* out);
+void qb_fill_boys_table(double* tab);   // QB_BOYS_TABLE_SIZE doubles, no allocation
 
 // Growable device array.
 template <class T>
@@ -107,6 +109,7 @@ struct qb_ctx {
     ClassLaunchers launch[QB_MAX_CLASS];
     int nclass = 0;
     int occ[QB_MAX_CLASS] = {};
+    int variant[QB_MAX_CLASS] = {};   // launcher variant per class (0 per-thread, 1 warp-cooperative)
     int class_bra[QB_MAX_CLASS] = {}, class_ket[QB_MAX_CLASS] = {};
     long long offs_off[QB_MAX_CLASS + 1] = {};
     DevArray<long long> d_offs;

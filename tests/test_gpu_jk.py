@@ -89,3 +89,48 @@ def test_benchmark_size_properties(qb):
     assert np.abs(J3 - J1 - J2).max() < 1e-8 * np.abs(J3).max()
     assert np.abs(K3 - K1 - K2).max() < 1e-8 * np.abs(K3).max()
     assert np.sum(D1 * J1) > 0 and np.sum(D1 * K1) > 0
+
+
+_VARIANT_SCRIPT = r"""
+import sys, numpy as np
+import __graft_entry__ as ge
+qb = ge.load_package()
+from quiqbox_gb300.workloads import random_shell_molecule, random_density
+out = {}
+for tag, kw in (("classes", dict(n_h=2, n_heavy=1, box=4.0, min_dist=1.0, seed=0)),
+                ("long", dict(n_h=1, n_heavy=1, box=3.0, min_dist=1.0, nprim=6, seed=5))):
+    atoms, coords, bs = random_shell_molecule(**kw)
+    fb = qb.flatten(bs)
+    D = random_density(fb.nfun, kw["seed"])
+    J, K = qb.jk(fb, D, schwarz=0.0)
+    out[tag + "_J"], out[tag + "_K"] = J, K
+np.savez(sys.argv[1], **out)
+"""
+
+
+@pytest.mark.parametrize("variant", ["thread", "warp"])
+def test_jk_kernel_variants(qb, oracle, tmp_path, variant):
+    # Both class-kernel variants (one contracted quartet per thread; warp-cooperative with
+    # pooled primitive quartets), selected per process through QB_JK_VARIANT.  "long" has
+    # 6-primitive shells: 36 primitive pairs per shell pair and up to 1296 primitive
+    # quartets per contracted quartet, beyond the warp kernel's tabulated counts (32) and
+    # its per-pass level window (256).
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    from quiqbox_gb300.workloads import random_shell_molecule, random_density
+    root = Path(__file__).resolve().parents[1]
+    out = tmp_path / f"jk_{variant}.npz"
+    env = dict(os.environ, QB_JK_VARIANT=variant)
+    subprocess.run([sys.executable, "-c", _VARIANT_SCRIPT, str(out)], cwd=root, env=env, check=True, timeout=600)
+    got = np.load(out)
+    for tag, kw, exact, tol in (("classes", dict(n_h=2, n_heavy=1, box=4.0, min_dist=1.0, seed=0), True, 1e-12),
+                                ("long", dict(n_h=1, n_heavy=1, box=3.0, min_dist=1.0, nprim=6, seed=5), False, 1e-10)):
+        atoms, coords, bs = random_shell_molecule(**kw)
+        fb = qb.flatten(bs)
+        D = random_density(fb.nfun, kw["seed"])
+        Jr, Kr = oracle.jk(fb, D, exact=exact)
+        scale = max(np.abs(Jr).max(), 1.0)
+        assert np.abs(got[tag + "_J"] - Jr).max() < tol * scale, tag
+        assert np.abs(got[tag + "_K"] - Kr).max() < tol * scale, tag

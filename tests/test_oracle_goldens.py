@@ -202,3 +202,13 @@ def test_reference_electron_transfer_round_off(qb, oracle):
     assert abs(exact[0] - exact[1]) < 1e-15
     assert abs(f64[1] - exact[1]) < 1e-14
     assert abs(f64[0] - exact[0]) > 1e-9
+
+
+def test_boys_at_x_equal_order_one(oracle):
+    # x = n = 1: the upper-order formula of BoysFunction.jl:27-31 diverges there; the
+    # oracle takes its limit (6n) and must still give F_1(1) exactly
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.dps = 40
+    ref = float(mpmath.quad(lambda t: t ** 2 * mpmath.exp(-t * t), [0, 1]))
+    assert oracle.boys(1.0, 1) == pytest.approx(ref, rel=1e-14)
+    assert oracle.boys_exact(1.0, 1) == pytest.approx(ref, rel=1e-15)
