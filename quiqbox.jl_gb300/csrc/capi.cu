@@ -57,17 +57,21 @@ int qb_create(qb_ctx** out, int device) {
         ctx->nclass = QB_NCLASS;
         qb_get_class_launchers(ctx->launch);
         // Variant per class: the generator's measured preference.  QB_JK_VARIANT overrides
-        // it for tuning: "thread", "warp", or one character per class ('t'/'w').
+        // it for tuning: "thread" (variant 0 everywhere), "warp" (variant 1 wherever
+        // compiled), or one character per class, '0'..'3' (a variant that is not compiled
+        // for a class falls back to the preference).
         const char* ov = getenv("QB_JK_VARIANT");
         for (int c = 0; c < ctx->nclass; ++c) {
             const ClassLaunchers& L = ctx->launch[c];
-            int v = (L.preferred && L.jk[1]) ? 1 : 0;
+            int v = L.preferred;
             if (ov) {
                 if (!strcmp(ov, "thread")) v = 0;
-                else if (strlen(ov) == (size_t)ctx->nclass) v = (ov[c] == 'w') ? 1 : 0;
-                v = (v && L.jk[1]) ? 1 : 0;
-                if (!strcmp(ov, "warp")) v = L.jk[1] ? 1 : 0;
+                else if (!strcmp(ov, "warp")) v = L.jk[1] ? 1 : 0;
+                else if (strlen(ov) == (size_t)ctx->nclass && ov[c] >= '0' && ov[c] < '0' + QB_NVARIANT &&
+                         L.jk[ov[c] - '0'])
+                    v = ov[c] - '0';
             }
+            if (!L.jk[v]) v = 0;
             ctx->variant[c] = v;
             ctx->occ[c] = L.occupancy[v]();
         }
@@ -96,7 +100,7 @@ void qb_destroy(qb_ctx* ctx) {
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     ctx->boys.release(); ctx->status.release();
     ctx->d_fp.release(); ctx->d_ijk.release(); ctx->d_cen.release(); ctx->d_alpha.release(); ctx->d_w.release();
-    ctx->d_ratio.release(); ctx->d_pairs.release(); ctx->d_prims.release(); ctx->d_Q.release(); ctx->d_npref.release();
+    ctx->d_ratio.release(); ctx->d_pairs.release(); ctx->d_prims.release(); ctx->d_prims32.release(); ctx->d_Q.release(); ctx->d_npref.release();
     ctx->d_offs.release(); ctx->d_stats.release(); ctx->d_primcount.release();
     ctx->d_D.release(); ctx->d_Dt.release(); ctx->d_Jp.release(); ctx->d_Kp.release(); ctx->d_J.release();
     ctx->d_K.release(); ctx->d_dmax.release();

@@ -266,6 +266,15 @@ __global__ void qb_primpair_compact_kernel(const ShellPair* __restrict__ pairs, 
     nkept[k] = kept;
 }
 
+// FP32 copy (p, P) of every primitive pair, read by the warp-cooperative class kernels
+// to group primitive quartets by Boys-function branch.
+__global__ void qb_primpair_f32_kernel(const PrimPair* __restrict__ prims, int n, float4* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const PrimPair& r = prims[k];
+    out[k] = make_float4((float)r.p, (float)r.Px, (float)r.Py, (float)r.Pz);
+}
+
 static int pc_index(int la, int lb) { return la * (la + 1) / 2 + lb; }
 
 int qb_ensure_pairs(qb_ctx* ctx) {
@@ -330,6 +339,8 @@ int qb_ensure_pairs(qb_ctx* ctx) {
                                                           ctx->d_w.p, ctx->d_prims.p, d_kmax.p);
     qb_primpair_compact_kernel<<<(npair + 127) / 128, 128, 0, s>>>(ctx->d_pairs.p, npair, ctx->d_prims.p, d_kmax.p,
                                                                   d_nkept.p);
+    QB_CUDA(ctx, ctx->d_prims32.ensure(nslot));
+    qb_primpair_f32_kernel<<<(nslot + 127) / 128, 128, 0, s>>>(ctx->d_prims.p, nslot, ctx->d_prims32.p);
     QB_CUDA(ctx, cudaGetLastError());
     {
         std::vector<int> nkept(npair);
@@ -528,7 +539,7 @@ int qb_jk_device(qb_ctx* ctx, const double* dD, double* dJ, double* dK, double t
         ClassWork w{ctx->d_pairs.p + plan.bra_off[c], ctx->d_pairs.p + plan.ket_off[c],
                     ctx->d_offs.p + plan.offs_off[c], plan.nbra[c], plan.same[c]};
         const int grid = ctx->nsm * std::max(1, ctx->occ[c]);
-        JKArgs args{ctx->d_prims.p, ctx->boys.p, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p, ctx->d_primcount.p + c, n};
+        JKArgs args{ctx->d_prims.p, ctx->d_prims32.p, ctx->boys.p, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p, ctx->d_primcount.p + c, n};
         ctx->launch[c].jk[ctx->variant[c]](w, args, grid, ctx->streams[k % QB_NSTREAM]);
         ++k;
     }

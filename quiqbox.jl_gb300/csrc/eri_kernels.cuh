@@ -19,6 +19,7 @@ struct ClassWork {
 
 struct JKArgs {
     const PrimPair* __restrict__ prims;
+    const float4* __restrict__ prims32;    // (p, Px, Py, Pz) of prims in FP32
     const double* __restrict__ boys;
     const double* __restrict__ D;          // ratio-scaled density, column-major
     double* Jp;                            // J' accumulator (column-major nfun x nfun)
@@ -162,33 +163,98 @@ __global__ void __launch_bounds__(128) qb_jk_class_kernel(const ClassWork w, con
 
 #define QB_WARP_MAXNB 32       // bra primitive pairs whose ket counts are tabulated (more: recounted)
 #define QB_WARP_MAXLEVEL 256   // primitive-quartet levels dealt out per pass
+#define QB_WARP_WINDOW 128     // primitive quartets regrouped by Boys branch at a time
+
+// Sum of the S accumulator rows of one owner (the HRR input).
+template <int S>
+struct QbRowSum {
+    const double* p;
+    int stride;
+    __device__ __forceinline__ double operator[](int k) const {
+        double v = p[k];
+#pragma unroll
+        for (int s = 1; s < S; ++s) v += p[s * stride + k];
+        return v;
+    }
+};
 
 // Warp-cooperative variant: a warp takes G <= 32 contracted quartets (one per "owner"
-// lane 0..G-1), pools all their significant primitive quartets and deals them out
-// evenly over its 32 lanes in level order (the s-th primitive quartet of every owner,
-// then the (s+1)-th, ...), so that the lanes of one round mostly serve distinct owners.
-// Each lane adds its primitive quartet's VRR targets to the owner's accumulator row in
-// shared memory as they are produced; the owners then run the HRR and the J/K
-// digestion.  Lane utilisation no longer depends on how many primitive quartets
-// survive the screening per contracted quartet, and the accumulators leave the
-// register file.
-template <int LA, int LB, int LC, int LD, int WPB, int G>
+// lane 0..G-1) and pools all their significant primitive quartets, dealt out evenly over
+// its 32 lanes in level order (the s-th primitive quartet of every owner, then the
+// (s+1)-th, ...).  REGROUP: every window of 128 pooled primitive quartets is first
+// regrouped so that those on the Boys table branch (T < QB_BOYS_TMAX, decided in FP32)
+// come before those on the asymptotic branch, and the warp runs one branch at a time.
+// Lanes of a round that serve the same owner write different accumulator rows (their
+// rank among them by __match_any_sync, capped at S-1) with atomicAdd; PLAIN: ranks
+// 0..S-2, alone on their row, add without atomics.  The owners finally sum their rows
+// and run the HRR and the J/K digestion.  Lane
+// utilisation no longer depends on how many primitive quartets survive the screening
+// per contracted quartet, and the accumulators leave the register file.
+template <int LA, int LB, int LC, int LD, int WPB, int G, int S, bool REGROUP, bool PLAIN>
 __global__ void __launch_bounds__(32 * WPB) qb_jk_warp_kernel(const ClassWork w, const JKArgs a) {
     using C = EriClass<LA, LB, LC, LD>;
     static_assert(G >= 1 && G <= 32, "owners per warp");
+    static_assert(S >= 1 && S <= 4, "accumulator rows per owner");
+    static_assert(!PLAIN || S >= 2, "plain adds need a shared overflow row");
     constexpr int NTP = C::NT | 1;
+    constexpr int ROW = G * NTP;                        // doubles between two rows of an owner
+    constexpr int W = REGROUP ? QB_WARP_WINDOW : 32;    // items regrouped per window
+    constexpr int NSUB = W / 32;
+    constexpr int WS = REGROUP ? W : 1;
     extern __shared__ double qb_dyn_smem[];
     __shared__ unsigned short s_cnt[WPB][G][QB_WARP_MAXNB];
     __shared__ int s_level[WPB][QB_WARP_MAXLEVEL + 1];
     __shared__ int s_prim0b[WPB][G], s_prim0k[WPB][G], s_nb[WPB][G], s_nk[WPB][G], s_tot[WPB][G];
     __shared__ unsigned char s_order[WPB][G];
+    __shared__ int s_wb[WPB][WS], s_wk[WPB][WS];        // window: bra / ket primitive-pair index
+    __shared__ unsigned char s_wo[WPB][WS];              // window: owner
     const unsigned FULL = 0xffffffffu;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double* acc = qb_dyn_smem + (size_t)warp * G * NTP;
+    const unsigned lanes_below = (1u << lane) - 1u;
+    double* acc = qb_dyn_smem + (size_t)warp * S * ROW;
     const long long total = __ldg(w.offs + w.nbra);
     const long long stride = (long long)gridDim.x * WPB * G;
     const float eps = (float)QB_PRIM_EPS;
     unsigned long long nprim_warp = 0;
+
+    // the owner's q-th significant primitive quartet -> (bra, ket) primitive-pair indices
+    auto decode = [&](int owner, int q, int& bpi, int& kpi) {
+        int ib = 0, rem = q;
+        if (s_nb[warp][owner] <= QB_WARP_MAXNB) {
+            while (rem >= s_cnt[warp][owner][ib]) { rem -= s_cnt[warp][owner][ib]; ++ib; }
+        } else {
+            const PrimPair* bp = a.prims + s_prim0b[warp][owner];
+            const PrimPair* kp = a.prims + s_prim0k[warp][owner];
+            const int nk = s_nk[warp][owner];
+            for (;;) {
+                const float kb = qb_kabs(bp + ib);
+                int n = 1;
+                while (n < nk && kb * qb_kabs(kp + n) >= eps) ++n;
+                if (rem < n) break;
+                rem -= n;
+                ++ib;
+            }
+        }
+        bpi = s_prim0b[warp][owner] + ib;
+        kpi = s_prim0k[warp][owner] + rem;
+    };
+    // one primitive quartet into the owner's accumulator rows (all lanes call it)
+    auto accumulate = [&](bool act, int owner, int bpi, int kpi) {
+        const unsigned same = __match_any_sync(FULL, act ? owner : 64 + lane);
+        const int rank = __popc(same & lanes_below);
+        if (act) {
+            const bool plain = PLAIN && rank < S - 1;
+            double* dst = acc + (size_t)min(rank, S - 1) * ROW + owner * NTP;
+            const PrimPair B = qb_load_pair(a.prims + bpi);
+            const PrimPair Kt = qb_load_pair(a.prims + kpi);
+            C::prim(B, Kt, a.boys, [&](int k, double v) {
+                if (plain) dst[k] += v;
+                else atomicAdd(dst + k, v);
+            });
+        }
+        __syncwarp();
+    };
+
     for (long long base = ((long long)blockIdx.x * WPB + warp) * G; base < total; base += stride) {
         const long long t = base + lane;
         const bool valid = lane < G && t < total;
@@ -230,7 +296,7 @@ __global__ void __launch_bounds__(32 * WPB) qb_jk_warp_kernel(const ClassWork w,
             s_order[warp][rank] = (unsigned char)lane;
             s_tot[warp][rank] = mytot;
         }
-        for (int e = lane; e < G * NTP; e += 32) acc[e] = 0.0;
+        for (int e = lane; e < S * ROW; e += 32) acc[e] = 0.0;
         __syncwarp();
         // levels [l0, l1) at a time: s_level[s - l0] = sum_k (min(count_k, s) - min(count_k, l0))
         for (int l0 = 0; l0 < maxtot; l0 += QB_WARP_MAXLEVEL) {
@@ -245,41 +311,82 @@ __global__ void __launch_bounds__(32 * WPB) qb_jk_warp_kernel(const ClassWork w,
             }
             __syncwarp();
             const int N = s_level[warp][l1 - l0];
-            for (int r = lane; r < N; r += 32) {
+            // pooled item r -> (owner, owner's primitive-quartet index)
+            auto item = [&](int r, int& owner, int& q) {
                 int lo = 0, hi = l1 - l0;   // s_level[lo] <= r < s_level[hi]
                 while (hi - lo > 1) {
                     const int mid = (lo + hi) >> 1;
                     if (s_level[warp][mid] <= r) lo = mid; else hi = mid;
                 }
-                const int owner = s_order[warp][r - s_level[warp][lo]];
-                // the owner's (l0 + lo)-th primitive quartet -> (bra ib, ket rem)
-                int ib = 0, rem = l0 + lo;
-                if (s_nb[warp][owner] <= QB_WARP_MAXNB) {
-                    while (rem >= s_cnt[warp][owner][ib]) { rem -= s_cnt[warp][owner][ib]; ++ib; }
-                } else {
-                    const PrimPair* bp = a.prims + s_prim0b[warp][owner];
-                    const PrimPair* kp = a.prims + s_prim0k[warp][owner];
-                    const int nk = s_nk[warp][owner];
-                    for (;;) {
-                        const float kb = qb_kabs(bp + ib);
-                        int n = 1;
-                        while (n < nk && kb * qb_kabs(kp + n) >= eps) ++n;
-                        if (rem < n) break;
-                        rem -= n;
-                        ++ib;
+                owner = s_order[warp][r - s_level[warp][lo]];
+                q = l0 + lo;
+            };
+            for (int w0 = 0; w0 < N; w0 += W) {
+                const int nw = min(W, N - w0);
+                if constexpr (REGROUP) {
+                    // regroup the window: Boys table branch first, asymptotic branch after
+                    int own[NSUB], bpi[NSUB], kpi[NSUB];
+                    unsigned tab[NSUB], vmask[NSUB];
+                    int ntab = 0;
+#pragma unroll
+                    for (int u = 0; u < NSUB; ++u) {
+                        const bool act = 32 * u + lane < nw;
+                        bool tb = false;
+                        own[u] = 0; bpi[u] = 0; kpi[u] = 0;
+                        if (act) {
+                            int q;
+                            item(w0 + 32 * u + lane, own[u], q);
+                            decode(own[u], q, bpi[u], kpi[u]);
+                            const float4 pb = __ldg(a.prims32 + bpi[u]);
+                            const float4 pk = __ldg(a.prims32 + kpi[u]);
+                            const float dx = pb.y - pk.y, dy = pb.z - pk.z, dz = pb.w - pk.w;
+                            const float T = __fdividef(pb.x * pk.x, pb.x + pk.x) * (dx * dx + dy * dy + dz * dz);
+                            tb = T < (float)QB_BOYS_TMAX;
+                        }
+                        tab[u] = __ballot_sync(FULL, tb);
+                        vmask[u] = __ballot_sync(FULL, act);
+                        ntab += __popc(tab[u]);
                     }
+                    int seen_tab = 0, seen_asy = 0;
+#pragma unroll
+                    for (int u = 0; u < NSUB; ++u) {
+                        const unsigned asy = vmask[u] & ~tab[u];
+                        if (vmask[u] & (1u << lane)) {
+                            const int pos = (tab[u] & (1u << lane)) ? seen_tab + __popc(tab[u] & lanes_below)
+                                                                    : ntab + seen_asy + __popc(asy & lanes_below);
+                            s_wb[warp][pos] = bpi[u];
+                            s_wk[warp][pos] = kpi[u];
+                            s_wo[warp][pos] = (unsigned char)own[u];
+                        }
+                        seen_tab += __popc(tab[u]);
+                        seen_asy += __popc(asy);
+                    }
+                    __syncwarp();
+#pragma unroll 1
+                    for (int u = 0; u < NSUB; ++u) {
+                        const int idx = 32 * u + lane;
+                        if (32 * u >= nw) break;
+                        const bool act = idx < nw;
+                        accumulate(act, act ? s_wo[warp][idx] : 0, act ? s_wb[warp][idx] : 0,
+                                   act ? s_wk[warp][idx] : 0);
+                    }
+                } else {
+                    const bool act = lane < nw;
+                    int owner = 0, bp = 0, kp = 0;
+                    if (act) {
+                        int q;
+                        item(w0 + lane, owner, q);
+                        decode(owner, q, bp, kp);
+                    }
+                    accumulate(act, owner, bp, kp);
                 }
-                const PrimPair B = qb_load_pair(a.prims + s_prim0b[warp][owner] + ib);
-                const PrimPair Kt = qb_load_pair(a.prims + s_prim0k[warp][owner] + rem);
-                double* dst = acc + owner * NTP;
-                C::prim(B, Kt, a.boys, [&](int k, double v) { atomicAdd(dst + k, v); });
             }
             if (lane == 0) nprim_warp += N;
             __syncwarp();
         }
         if (valid) {
             double I[C::NINT];
-            C::hrr(acc + lane * NTP, P.ABx, P.ABy, P.ABz, Q.ABx, Q.ABy, Q.ABz, I);
+            C::hrr(QbRowSum<S>{acc + lane * NTP, ROW}, P.ABx, P.ABy, P.ABz, Q.ABx, Q.ABy, Q.ABz, I);
             const double deg = (P.same ? 1.0 : 2.0) * (Q.same ? 1.0 : 2.0) * ((w.same && i == j) ? 1.0 : 2.0);
             qb_jk_digest<C>(P, Q, deg, a, I);
         }
@@ -290,15 +397,14 @@ __global__ void __launch_bounds__(32 * WPB) qb_jk_warp_kernel(const ClassWork w,
 }
 
 // Host-side launchers, one set per class (defined in the generated eri_class_*.cu).
-// Variant 0 runs one contracted quartet per thread (qb_jk_class_kernel); variant 1 the
-// warp-cooperative kernel (qb_jk_warp_kernel), present when its accumulators fit in
-// shared memory (warps_per_block > 0).
+// Variant 0 runs one contracted quartet per thread (qb_jk_class_kernel); variants 1..3
+// are configurations of the warp-cooperative kernel (null where not compiled).
+#define QB_NVARIANT 4
 struct ClassLaunchers {
-    void (*jk[2])(const ClassWork&, const JKArgs&, int grid, cudaStream_t);
-    int (*occupancy[2])(void);   // resident blocks per SM (also sets the shared-memory limit)
+    void (*jk[QB_NVARIANT])(const ClassWork&, const JKArgs&, int grid, cudaStream_t);
+    int (*occupancy[QB_NVARIANT])(void);   // resident blocks per SM (also sets the shared-memory limit)
     int la, lb, lc, ld;
-    int warps_per_block;
-    int preferred;               // default variant
+    int preferred;                         // default variant
 };
 
 #define QB_DEFINE_LAUNCHERS(LA, LB, LC, LD)                                                                  \
@@ -311,20 +417,22 @@ struct ClassLaunchers {
         return nb;                                                                                           \
     }
 
-#define QB_WARP_SMEM(LA, LB, LC, LD, WPB, G) \
-    ((size_t)(WPB) * (G) * (EriClass<LA, LB, LC, LD>::NT | 1) * sizeof(double))
+#define QB_WARP_SMEM(LA, LB, LC, LD, WPB, G, S) \
+    ((size_t)(WPB) * (S) * (G) * (EriClass<LA, LB, LC, LD>::NT | 1) * sizeof(double))
 
-#define QB_DEFINE_WARP_LAUNCHERS(LA, LB, LC, LD, WPB, G)                                                      \
-    static void qb_jkw_launch_##LA##LB##LC##LD(const ClassWork& w, const JKArgs& a, int grid, cudaStream_t s) { \
-        qb_jk_warp_kernel<LA, LB, LC, LD, WPB, G>                                                               \
-            <<<grid, 32 * (WPB), QB_WARP_SMEM(LA, LB, LC, LD, WPB, G), s>>>(w, a);                              \
+// Warp-kernel configuration V of class LA LB LC LD.
+#define QB_DEFINE_WARP_LAUNCHERS(V, LA, LB, LC, LD, WPB, G, S, RG, PL)                                       \
+    static void qb_jkw##V##_launch_##LA##LB##LC##LD(const ClassWork& w, const JKArgs& a, int grid,          \
+                                                    cudaStream_t s) {                                        \
+        qb_jk_warp_kernel<LA, LB, LC, LD, WPB, G, S, RG, PL>                                                 \
+            <<<grid, 32 * (WPB), QB_WARP_SMEM(LA, LB, LC, LD, WPB, G, S), s>>>(w, a);                        \
     }                                                                                                        \
-    static int qb_occw_##LA##LB##LC##LD(void) {                                                              \
-        cudaFuncSetAttribute(qb_jk_warp_kernel<LA, LB, LC, LD, WPB, G>,                                          \
+    static int qb_occw##V##_##LA##LB##LC##LD(void) {                                                         \
+        cudaFuncSetAttribute(qb_jk_warp_kernel<LA, LB, LC, LD, WPB, G, S, RG, PL>,                            \
                              cudaFuncAttributeMaxDynamicSharedMemorySize,                                    \
-                             (int)QB_WARP_SMEM(LA, LB, LC, LD, WPB, G));                                        \
+                             (int)QB_WARP_SMEM(LA, LB, LC, LD, WPB, G, S));                                  \
         int nb = 0;                                                                                          \
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, qb_jk_warp_kernel<LA, LB, LC, LD, WPB, G>, 32 * (WPB), \
-                                                      QB_WARP_SMEM(LA, LB, LC, LD, WPB, G));                    \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, qb_jk_warp_kernel<LA, LB, LC, LD, WPB, G, S, RG, PL>, \
+                                                      32 * (WPB), QB_WARP_SMEM(LA, LB, LC, LD, WPB, G, S));  \
         return nb;                                                                                           \
     }

@@ -411,20 +411,36 @@ class ClassGen:
         return "\n".join(o)
 
 
-# Warp-cooperative kernel: 4 warps per block, one block per SM; each warp holds the
-# accumulator rows ((NT | 1) doubles) of G owner quartets in shared memory, G <= 32,
-# within 50 KiB per warp (the rest of the 227 KiB is the kernel's static tables).
+# Warp-cooperative kernel: 4 warps per block; each warp holds S rows of accumulators
+# ((NT | 1) doubles each) for G <= 32 owner quartets in shared memory, within 50 KiB per
+# warp (the rest of the 227 KiB is the kernel's static tables).  Configurations, as
+# (S, regroup by Boys branch, plain adds for ranks < S-1):
+#   1: S = 1, no regrouping (every add atomic; G = 32 where one row per owner fits)
+#   2: S = 4 rows where they fit (else 3, 2), regrouping, plain adds
+#   3: S = 2, regrouping, every add atomic
 WARPS_PER_BLOCK = 4
 SMEM_PER_WARP = 50 * 1024
 
+# Default variant per class (0: per-thread kernel), measured on GB300 with the J/K build
+# of 64 H + 16 C/N/O, 3-primitive s/p/d shells.  Classes not listed use variant 1.
+PREFERRED = {"2121": 0, "2211": 0, "2221": 0,
+             "0000": 2, "1000": 2, "1010": 2, "1100": 2, "2000": 2, "2010": 2, "2100": 2,
+             "1110": 3, "2020": 3}
 
-# Classes whose per-thread kernel measured faster on GB300 than the warp-cooperative one
-# (J/K build of 64 H + 16 C/N/O, 3-primitive s/p/d shells): launched per thread by default.
-PREFER_PER_THREAD = {"2121", "2211", "2221"}
 
-
-def owners_per_warp(nt):
-    return max(0, min(32, SMEM_PER_WARP // ((nt | 1) * 8)))
+def warp_configs(nt):
+    """{variant: (G, S, regroup, plain)} of the warp kernel for a class with NT targets."""
+    rows = SMEM_PER_WARP // ((nt | 1) * 8)
+    if rows < 1:
+        return {}
+    if rows < 32:
+        return {1: (rows, 1, False, False)}
+    cfg = {1: (32, 1, False, False)}
+    s_max = min(4, rows // 32)
+    if s_max >= 2:
+        cfg[2] = (32, s_max, True, True)
+        cfg[3] = (32, 2, True, False)
+    return cfg
 
 
 HEADER = """// GENERATED by gen_eri.py -- do not edit.
@@ -445,19 +461,24 @@ def main(outdir, lmax=LMAX_DEFAULT):
         (outdir / f"eri_class_{name}.cuh").write_text(HEADER + code + "\n")
         la, lb, lc, ld = cls
         nt = len(g.esets) * len(g.fsets)
-        g_own = owners_per_warp(nt)
-        wpb = WARPS_PER_BLOCK if g_own else 0
+        cfgs = warp_configs(nt)
         cu = [f'// GENERATED by gen_eri.py -- do not edit.',
               f'#include "eri_class_{name}.cuh"', '#include "eri_kernels.cuh"',
               f'QB_DEFINE_LAUNCHERS({la}, {lb}, {lc}, {ld})']
-        if wpb:
-            cu.append(f'QB_DEFINE_WARP_LAUNCHERS({la}, {lb}, {lc}, {ld}, {wpb}, {g_own})')
-            wj, wo = f'qb_jkw_launch_{name}', f'qb_occw_{name}'
-        else:
-            wj, wo = 'nullptr', 'nullptr'
-        pref = 1 if (wpb and name not in PREFER_PER_THREAD) else 0
-        cu.append(f"ClassLaunchers qb_class_{name}() {{ return {{{{qb_jk_launch_{name}, {wj}}}, "
-                  f"{{qb_occ_{name}, {wo}}}, {la}, {lb}, {lc}, {ld}, {wpb}, {pref}}}; }}")
+        jk, occ = [f"qb_jk_launch_{name}"], [f"qb_occ_{name}"]
+        for v in (1, 2, 3):
+            if v in cfgs:
+                G_, S_, rg, pl = cfgs[v]
+                cu.append(f"QB_DEFINE_WARP_LAUNCHERS({v}, {la}, {lb}, {lc}, {ld}, {WARPS_PER_BLOCK}, {G_}, {S_}, "
+                          f"{'true' if rg else 'false'}, {'true' if pl else 'false'})")
+                jk.append(f"qb_jkw{v}_launch_{name}")
+                occ.append(f"qb_occw{v}_{name}")
+            else:
+                jk.append("nullptr")
+                occ.append("nullptr")
+        pref = PREFERRED.get(name, 1 if 1 in cfgs else 0)
+        cu.append(f"ClassLaunchers qb_class_{name}() {{ return {{{{{', '.join(jk)}}}, {{{', '.join(occ)}}}, "
+                  f"{la}, {lb}, {lc}, {ld}, {pref}}}; }}")
         (outdir / f"eri_class_{name}.cu").write_text("\n".join(cu) + "\n")
         files.append(name)
         table[name] = {"prim_flops": g.prim.flops(), "contr_flops": g.contr.flops(),

@@ -101,6 +101,7 @@ struct qb_ctx {
     std::vector<ShellPair> h_pairs;      // sorted by pair class then descending Q
     DevArray<ShellPair> d_pairs;
     DevArray<PrimPair> d_prims;
+    DevArray<float4> d_prims32;   // (p, Px, Py, Pz) of d_prims in FP32 (Boys-branch grouping)
     DevArray<double> d_Q;                 // per pair, sorted like d_pairs
     DevArray<long long> d_npref;          // per pair class: exclusive prefix of nprim (segment of size n+1)
     int npref_off[QB_MAX_PC + 1] = {};

@@ -108,10 +108,11 @@ np.savez(sys.argv[1], **out)
 """
 
 
-@pytest.mark.parametrize("variant", ["thread", "warp"])
+@pytest.mark.parametrize("variant", ["thread", "warp", "2" * 21, "3" * 21])
 def test_jk_kernel_variants(qb, oracle, tmp_path, variant):
-    # Both class-kernel variants (one contracted quartet per thread; warp-cooperative with
-    # pooled primitive quartets), selected per process through QB_JK_VARIANT.  "long" has
+    # Every class-kernel variant (one contracted quartet per thread; the configurations of
+    # the warp-cooperative kernel with pooled primitive quartets), selected per process
+    # through QB_JK_VARIANT.  "long" has
     # 6-primitive shells: 36 primitive pairs per shell pair and up to 1296 primitive
     # quartets per contracted quartet, beyond the warp kernel's tabulated counts (32) and
     # its per-pass level window (256).
@@ -121,7 +122,7 @@ def test_jk_kernel_variants(qb, oracle, tmp_path, variant):
     from pathlib import Path
     from quiqbox_gb300.workloads import random_shell_molecule, random_density
     root = Path(__file__).resolve().parents[1]
-    out = tmp_path / f"jk_{variant}.npz"
+    out = tmp_path / f"jk_{variant[:6]}.npz"
     env = dict(os.environ, QB_JK_VARIANT=variant)
     subprocess.run([sys.executable, "-c", _VARIANT_SCRIPT, str(out)], cwd=root, env=env, check=True, timeout=600)
     got = np.load(out)
