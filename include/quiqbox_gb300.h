@@ -67,6 +67,13 @@ int qb_nuc_attractions(qb_ctx* ctx, const qb_basis* basis, int nnuc, const doubl
 int qb_core_hamiltonian(qb_ctx* ctx, const qb_basis* basis, int nnuc, const double* Z, const double* R,
                         double* H);
 
+/* Multipole moments M_ij = <i| (x-Cx)^nx (y-Cy)^ny (z-Cz)^nz |j>, nfun x nfun, column-major.
+ * Replaces multipoleMoments (src/Integration/Interface.jl:95; sampler Samplers.jl:19-21,
+ * primitive integrals GaussianOrbitals.jl:184-247).  degrees[k] >= 0; per axis the left
+ * and right Cartesian powers plus degrees[k] may not exceed 26 (QB_ERR_UNSUPPORTED). */
+int qb_multipole_moments(qb_ctx* ctx, const qb_basis* basis, const double center[3], const int degrees[3],
+                         double* M);
+
 /* Boys function sequence on the device: F[i*(M+1) + m] = F_m(T[i]), m = 0..M, T[i] >= 0.
  * Replaces computeBoysSequence (src/Integration/Engines/BoysFunction.jl:67-77) and
  * computeBoysFunc (:62-64).  path 0: the evaluator of the ERI class kernels (M <= 8);
@@ -165,7 +172,7 @@ int qb_fp64_peak(qb_ctx* ctx, double* tflops);
  * alpha, weight), dD is the nfun x nfun density, dJ / dK receive the results;
  * `stream` is a cudaStream_t (NULL = legacy default stream).  No Schwarz screening.
  *  - Limit: nfun <= 512; larger bases return QB_ERR_DIM before touching any pointer.
- *  - Scratch: a file-scope device array of 4 MiB (+ a 1.7 MiB Boys table) held by
+ * *  - Scratch: a file-scope device array of 4 MiB (+ a 2.1 MiB Boys table) held by
  *    every GPU that loads the library until exit.  The first call on a device does
  *    the set-up (resolves the arrays' device addresses, uploads the Boys table) and
  *    must come before any stream capture on that device.

@@ -51,6 +51,7 @@ def lib():
             getattr(L, "qbo_eri_tensor" + sfx).argtypes = basis + [_pd]
             getattr(L, "qbo_eri_list" + sfx).argtypes = basis + [_i64, _pi, _pd]
             getattr(L, "qbo_jk_list" + sfx).argtypes = basis + [_i64, _pi, _pd, _pd, _pd, _pd, _i]
+            getattr(L, "qbo_multipole" + sfx).argtypes = basis + [_pd, _pi, _pd]
         L.qbo_boys_q.restype = _d
         L.qbo_boys_q.argtypes = [_d, _i]
         L.qbo_num_threads.restype = _i
@@ -134,6 +135,14 @@ def kinetics(fb, exact=False):
 
 def nuc_attractions(fb, Z, R, exact=False):
     return _one_body(2, fb, Z, R, exact=exact)
+
+
+def multipoles(fb, center, degrees, exact=False):
+    """multipoleMoments(center, degrees, basis) (Interface.jl:95), nfun x nfun."""
+    n = fb.nfun
+    buf = np.zeros(n * n)
+    getattr(lib(), "qbo_multipole" + _sfx(exact))(*_b(fb), _v(center), _v(degrees, np.int32), buf)
+    return buf.reshape((n, n), order="F").copy()
 
 
 def eri_tensor(fb, exact=False):

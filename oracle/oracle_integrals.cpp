@@ -302,6 +302,53 @@ R prim_overlap(const Product<R>& d) {
     return r;
 }
 
+// computePGTOrbMultipoleMoment (GaussianOrbitals.jl:184-202): a primitive with itself,
+// monomial prod_k (x_k - C_k)^n_k
+template <class R>
+R prim_multipole_sym(const Prim<R>& p, const R C[3], const int n[3]) {
+    R res = 1;
+    for (int k = 0; k < 3; ++k) {
+        const R dx = p.c[k] - C[k];
+        const int m = (dx == 0) ? 0 : n[k];
+        R temp = 0;
+        for (int q = 0; q <= m; ++q) {
+            const int l = n[k] - q;
+            if (l % 2 == 0) temp += (R)binom(n[k], q) * ipow(dx, q) * axial_factor(2 * p.a, p.l[k] + (l >> 1));
+        }
+        res *= temp;
+    }
+    return res;
+}
+
+// computePGTOrbMultipoleMoment! (GaussianOrbitals.jl:204-247): binomial expansion of
+// (x - C)^n about the right centre (or the left one when C sits on it)
+template <class R>
+R prim_multipole(const Product<R>& d, const R C[3], const int n[3]) {
+    if (n[0] + n[1] + n[2] == 0) return prim_overlap(d);
+    if (d.sym) return prim_multipole_sym(d.L, C, n);
+    const R xpos = d.L.a * d.Rt.a / d.xpn;
+    R res = 1;
+    for (int k = 0; k < 3; ++k) {
+        R xL = d.L.c[k], xR = d.Rt.c[k];
+        int iL = d.L.l[k], iR = d.Rt.l[k];
+        const R dx = xR - C[k];
+        int m = n[k];
+        if (dx == 0) {
+            m = 0;
+        } else if (xL == C[k]) {
+            std::swap(xL, xR);
+            std::swap(iL, iR);
+            m = 0;
+        }
+        R temp = 0;
+        for (int q = 0; q <= m; ++q)
+            temp += (R)binom(n[k], q) * ipow(dx, q) *
+                    axial_overlap(d.xpn, xpos, d.cen[k] - xL, d.cen[k] - xR, iL, iR + n[k] - q);
+        res *= temp;
+    }
+    return res;
+}
+
 // computeAxialPGTOrbCoordDiff! (GaussianOrbitals.jl:258-281)
 template <class R>
 R axial_diff(int degree, R xL, R xR, R xML, R xMR, int iL, int iR) {
@@ -587,6 +634,19 @@ R contracted_1e(const Basis& b, int i, int j, int kind, int nnuc, const double* 
     return res;
 }
 
+// getOrbLayoutIntegralCore! one-body with the multipole sampler (Framework.jl:505-523,
+// Samplers.jl:19-21)
+template <class R>
+R contracted_multipole(const Basis& b, int i, int j, const R C[3], const int n[3]) {
+    R res = 0;
+    for (int pr = b.fp[j]; pr < b.fp[j + 1]; ++pr)
+        for (int pl = b.fp[i]; pl < b.fp[i + 1]; ++pl) {
+            const Product<R> d = make_product(b.prim<R>(pl), b.prim<R>(pr));
+            res += prim_multipole(d, C, n) * ((R)b.w[pl] * (R)b.w[pr]);
+        }
+    return res;
+}
+
 // getOrbLayoutIntegralCore! two-body (Framework.jl:526-554): Σ w·w·w·w (ab|cd)
 template <class R>
 R contracted_eri(const Basis& b, int i, int j, int k, int l) {
@@ -683,6 +743,21 @@ Product<R> prod_of(const double* A, double a, const int* la, const double* B, do
     return make_product(make_prim<R>(A, a, la), make_prim<R>(B, b, lb));
 }
 
+// multipoleMoments (Interface.jl:95): nfun x nfun, column-major, both triangles
+// (getOrbVectorIntegralCore! one-body, Framework.jl:581-607).
+template <class R>
+void multipole_matrix(const Basis& b, const double* C, const int* n, double* out) {
+    const R Cr[3] = {(R)C[0], (R)C[1], (R)C[2]};
+    const int N = b.nfun;
+#pragma omp parallel for schedule(dynamic)
+    for (int j = 0; j < N; ++j)
+        for (int i = 0; i <= j; ++i) {
+            const double v = (double)contracted_multipole<R>(b, i, j, Cr, n);
+            out[i + (size_t)N * j] = v;
+            out[j + (size_t)N * i] = v;
+        }
+}
+
 }  // namespace
 
 extern "C" {
@@ -715,6 +790,15 @@ void qbo_one_body(int kind, int nfun, const int* fp, const double* cen, const in
 void qbo_one_body_q(int kind, int nfun, const int* fp, const double* cen, const int* ijk, const double* alpha,
                     const double* w, int nnuc, const double* Z, const double* R, double* out) {
     one_body<quad>(kind, Basis{nfun, fp, cen, ijk, alpha, w}, nnuc, Z, R, out);
+}
+
+void qbo_multipole(int nfun, const int* fp, const double* cen, const int* ijk, const double* alpha,
+                   const double* w, const double* C, const int* n, double* out) {
+    multipole_matrix<double>(Basis{nfun, fp, cen, ijk, alpha, w}, C, n, out);
+}
+void qbo_multipole_q(int nfun, const int* fp, const double* cen, const int* ijk, const double* alpha,
+                     const double* w, const double* C, const int* n, double* out) {
+    multipole_matrix<quad>(Basis{nfun, fp, cen, ijk, alpha, w}, C, n, out);
 }
 
 // getOrbVectorIntegralCore! two-body with the 8-fold scatter (Framework.jl:640-666).

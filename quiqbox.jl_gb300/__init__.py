@@ -12,6 +12,6 @@ from .basis import (PrimitiveOrb, CompositeOrb, NuclearCluster, FlatBasis, genGa
 from .api import (overlaps, overlap, elecKinetics, elecKinetic, nucAttractions, nucAttraction,  # noqa: F401
                   coreHamiltonian, elecRepulsions, elecRepulsion, elecRepulsion_list, jk, SCFconfig,
                   HFconfig, HFfinalInfo, runHartreeFock, RCHartreeFock, UOHartreeFock, fp64_peak, device_info,
-                  computeBoysSequence, computeBoysFunc,
+                  computeBoysSequence, computeBoysFunc, multipoleMoments, multipoleMoment,
                   DimensionMismatch, DomainError)
 from ._lib import Context, load as load_library, LIB_PATH, EXPORTED  # noqa: F401

@@ -20,7 +20,7 @@ QB_OK, QB_ERR_ARG, QB_ERR_DIM, QB_ERR_DOMAIN, QB_ERR_CUDA, QB_ERR_TIMEOUT, QB_ER
 EXPORTED = ["qb_create", "qb_destroy", "qb_last_error", "qb_device_info", "qb_overlaps", "qb_elec_kinetics",
             "qb_nuc_attractions", "qb_core_hamiltonian", "qb_elec_repulsions", "qb_elec_repulsion_list", "qb_jk",
             "qb_jk_prepare", "qb_jk_upload_density", "qb_jk_execute", "qb_jk_download", "qb_jk_get_stats", "qb_jk_pair_table",
-            "qb_scf_config_default", "qb_run_hartree_fock", "qb_fp64_peak", "qb_jk_noalloc", "qb_boys"]
+            "qb_scf_config_default", "qb_run_hartree_fock", "qb_fp64_peak", "qb_jk_noalloc", "qb_boys", "qb_multipole_moments"]
 
 
 class DimensionMismatch(ValueError):

@@ -67,6 +67,19 @@ def overlap(b1, b2, ctx=None):
     return overlaps([b1, b2], ctx)[0, 1]
 
 
+def multipoleMoments(center, degrees, basis, ctx=None):
+    """M_ij = <i| prod_k (x_k - C_k)^{n_k} |j> (Interface.jl:95)."""
+    fb = _flat(basis)
+    C3 = np.ascontiguousarray(np.asarray(center, dtype=np.float64).reshape(3))
+    n3 = np.ascontiguousarray(np.asarray(degrees, dtype=np.int32).reshape(3))
+    return _matrix(_ctx(ctx).lib.qb_multipole_moments, fb, ctx, L.dptr(C3), L.iptr(n3))
+
+
+def multipoleMoment(center, degrees, b1, b2, ctx=None):
+    """<b1| prod_k (x_k - C_k)^{n_k} |b2> (Interface.jl:71)."""
+    return multipoleMoments(center, degrees, [b1, b2], ctx)[0, 1]
+
+
 def elecKinetics(basis, ctx=None):
     """T_ij = <i|-1/2 ∇²|j> (Interface.jl:143)."""
     return _matrix(_ctx(ctx).lib.qb_elec_kinetics, _flat(basis), ctx)

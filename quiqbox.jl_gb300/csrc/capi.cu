@@ -150,6 +150,23 @@ int qb_core_hamiltonian(qb_ctx* ctx, const qb_basis* basis, int nnuc, const doub
     return onebody_api(ctx, basis, 6, nnuc, Z, R, H);
 }
 
+int qb_multipole_moments(qb_ctx* ctx, const qb_basis* basis, const double* center, const int* degrees, double* M) {
+    QB_TRY(enter(ctx));
+    if (!M || !center || !degrees) return qb_set_error(ctx, QB_ERR_ARG, "null argument");
+    for (int k = 0; k < 3; ++k) {
+        if (!std::isfinite(center[k])) return qb_set_error(ctx, QB_ERR_DOMAIN, "non-finite multipole centre");
+        if (degrees[k] < 0) return qb_set_error(ctx, QB_ERR_DOMAIN, "negative multipole degree");
+    }
+    QB_TRY(qb_set_basis(ctx, basis));
+    const size_t nn = (size_t)ctx->nfun * ctx->nfun;
+    QB_CUDA(ctx, ctx->d_m0.ensure(nn));
+    if (qb_gen_multipole(qb_gen_basis(ctx), center, degrees, ctx->d_m0.p, ctx->status.p, ctx->stream) != 0)
+        return qb_cuda_check(ctx, cudaGetLastError(), "multipole kernel");
+    QB_CUDA(ctx, cudaMemcpyAsync(M, ctx->d_m0.p, nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    QB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return qb_check_status(ctx);
+}
+
 int qb_elec_repulsions(qb_ctx* ctx, const qb_basis* basis, double* eri) {
     QB_TRY(enter(ctx));
     if (!eri) return qb_set_error(ctx, QB_ERR_ARG, "null output");

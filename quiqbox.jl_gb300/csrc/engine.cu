@@ -80,20 +80,15 @@ static std::vector<std::array<int, 3>> cart_components(int L) {
     return out;
 }
 
-// Groups consecutive functions into Cartesian shells: same centre, exponents and
-// primitive count, powers in SubshellXYZs order (src/Lexicons.jl:17-36), and
-// weights that factor as ratio(function) * coefficient(primitive).
-static void detect_shells(qb_ctx* ctx) {
-    ctx->shells.clear();
-    ctx->h_ratio.assign(ctx->nfun, 1.0);
-    ctx->shell_path = true;
-    const int* fp = ctx->h_fp.data();
-    const double* cen = ctx->h_cen.data();
-    const int* ijk = ctx->h_ijk.data();
-    const double* al = ctx->h_alpha.data();
-    const double* w = ctx->h_w.data();
-    int f = 0;
-    while (f < ctx->nfun) {
+// Groups the consecutive functions [f_begin, f_end) into Cartesian shells: same centre,
+// exponents and primitive count, powers in SubshellXYZs order (src/Lexicons.jl:17-36),
+// and weights that factor as ratio(function) * coefficient(primitive).  Appends the
+// shells and writes ratio[f]; returns false (shells/ratios partially written) if the
+// functions are not shell-structured or L > QB_LMAX_SHELL.
+bool qb_detect_shells(int f_begin, int f_end, const int* fp, const double* cen, const int* ijk, const double* al,
+                      const double* w, std::vector<HostShell>& shells, double* ratio) {
+    int f = f_begin;
+    while (f < f_end) {
         const int p0 = fp[f], K = fp[f + 1] - fp[f];
         bool ok = K > 0;
         int L = ok ? ijk[3 * p0] + ijk[3 * p0 + 1] + ijk[3 * p0 + 2] : -1;
@@ -101,7 +96,7 @@ static void detect_shells(qb_ctx* ctx) {
         std::vector<std::array<int, 3>> comps;
         if (ok) comps = cart_components(L);
         const int nc = ok ? (int)comps.size() : 0;
-        ok = ok && f + nc <= ctx->nfun;
+        ok = ok && f + nc <= f_end;
         for (int c = 0; ok && c < nc; ++c) {
             const int g = f + c, q0 = fp[g];
             if (fp[g + 1] - q0 != K) { ok = false; break; }
@@ -116,22 +111,29 @@ static void detect_shells(qb_ctx* ctx) {
                 }
                 if (w[pa] == 0.0 || std::fabs(w[pb] - r * w[pa]) > 1e-13 * std::fabs(w[pb])) ok = false;
             }
-            if (ok) ctx->h_ratio[g] = r;
+            if (ok) ratio[g] = r;
         }
-        if (!ok) {
-            ctx->shell_path = false;
-            ctx->shells.clear();
-            ctx->h_ratio.assign(ctx->nfun, 1.0);
-            return;
-        }
+        if (!ok) return false;
         HostShell s;
         for (int x = 0; x < 3; ++x) s.c[x] = cen[3 * p0 + x];
         s.L = L;
         s.K = K;
         s.prim0 = p0;
         s.f0 = f;
-        ctx->shells.push_back(s);
+        shells.push_back(s);
         f += nc;
+    }
+    return true;
+}
+
+static void detect_shells(qb_ctx* ctx) {
+    ctx->shells.clear();
+    ctx->h_ratio.assign(ctx->nfun, 1.0);
+    ctx->shell_path = qb_detect_shells(0, ctx->nfun, ctx->h_fp.data(), ctx->h_cen.data(), ctx->h_ijk.data(),
+                                       ctx->h_alpha.data(), ctx->h_w.data(), ctx->shells, ctx->h_ratio.data());
+    if (!ctx->shell_path) {
+        ctx->shells.clear();
+        ctx->h_ratio.assign(ctx->nfun, 1.0);
     }
 }
 
@@ -207,9 +209,6 @@ int qb_check_status(qb_ctx* ctx) {
 
 // ---------------------------------------------------------------------------
 // Shell pairs and primitive pairs.
-struct PairSlot {
-    int sa, sb, pa, pb;   // shells and shell-primitive indices (into the flattened basis)
-};
 
 __global__ void qb_primpair_kernel(const PairSlot* __restrict__ slots, int n, const double* __restrict__ cen,
                                    const double* __restrict__ alpha, const double* __restrict__ w,
@@ -275,6 +274,20 @@ __global__ void qb_primpair_f32_kernel(const PrimPair* __restrict__ prims, int n
     out[k] = make_float4((float)r.p, (float)r.Px, (float)r.Py, (float)r.Pz);
 }
 
+// Primitive pairs of every slot, sorted and compacted per shell pair (nkept), plus their
+// FP32 centres.  d_kmax is scratch (one word).
+int qb_build_prim_pairs(cudaStream_t s, const PairSlot* d_slots, int nslot, const double* d_cen,
+                        const double* d_alpha, const double* d_w, const ShellPair* d_pairs, int npair,
+                        PrimPair* d_prims, float4* d_prims32, int* d_nkept, unsigned long long* d_kmax) {
+    if (cudaMemsetAsync(d_kmax, 0, sizeof(unsigned long long), s) != cudaSuccess) return -1;
+    if (nslot > 0)
+        qb_primpair_kernel<<<(nslot + 127) / 128, 128, 0, s>>>(d_slots, nslot, d_cen, d_alpha, d_w, d_prims, d_kmax);
+    if (npair > 0)
+        qb_primpair_compact_kernel<<<(npair + 127) / 128, 128, 0, s>>>(d_pairs, npair, d_prims, d_kmax, d_nkept);
+    if (nslot > 0) qb_primpair_f32_kernel<<<(nslot + 127) / 128, 128, 0, s>>>(d_prims, nslot, d_prims32);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 static int pc_index(int la, int lb) { return la * (la + 1) / 2 + lb; }
 
 int qb_ensure_pairs(qb_ctx* ctx) {
@@ -334,14 +347,10 @@ int qb_ensure_pairs(qb_ctx* ctx) {
     DevArray<int> d_nkept;
     QB_CUDA(ctx, d_kmax.ensure(1));
     QB_CUDA(ctx, d_nkept.ensure(npair));
-    QB_CUDA(ctx, cudaMemsetAsync(d_kmax.p, 0, sizeof(unsigned long long), s));
-    qb_primpair_kernel<<<(nslot + 127) / 128, 128, 0, s>>>(d_slots.p, nslot, ctx->d_cen.p, ctx->d_alpha.p,
-                                                          ctx->d_w.p, ctx->d_prims.p, d_kmax.p);
-    qb_primpair_compact_kernel<<<(npair + 127) / 128, 128, 0, s>>>(ctx->d_pairs.p, npair, ctx->d_prims.p, d_kmax.p,
-                                                                  d_nkept.p);
     QB_CUDA(ctx, ctx->d_prims32.ensure(nslot));
-    qb_primpair_f32_kernel<<<(nslot + 127) / 128, 128, 0, s>>>(ctx->d_prims.p, nslot, ctx->d_prims32.p);
-    QB_CUDA(ctx, cudaGetLastError());
+    if (qb_build_prim_pairs(s, d_slots.p, nslot, ctx->d_cen.p, ctx->d_alpha.p, ctx->d_w.p, ctx->d_pairs.p, npair,
+                            ctx->d_prims.p, ctx->d_prims32.p, d_nkept.p, d_kmax.p) != 0)
+        return qb_cuda_check(ctx, cudaGetLastError(), "primitive pairs");
     {
         std::vector<int> nkept(npair);
         QB_CUDA(ctx, cudaMemcpyAsync(nkept.data(), d_nkept.p, npair * sizeof(int), cudaMemcpyDeviceToHost, s));

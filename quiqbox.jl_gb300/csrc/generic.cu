@@ -94,16 +94,12 @@ __device__ __forceinline__ void tri_decode(long long n, int& i, int& j) {   // n
     j = (int)(n - a * (a + 1) / 2);
 }
 
-// One-electron matrices: one thread per function pair i >= j.
-// flags: 1 overlap, 2 kinetic, 4 nuclear attraction.  Outputs column-major, both triangles.
-__global__ void qb_onebody_kernel(const GenBasis b, int flags, int nnuc, const double* __restrict__ Z,
-                                  const double* __restrict__ Rn, const double* __restrict__ boys,
-                                  double* S, double* T, double* V, int* status) {
-    const long long npair = (long long)b.nfun * (b.nfun + 1) / 2;
-    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= npair) return;
-    int fi, fj;
-    tri_decode(n, fi, fj);
+// One-electron integrals of the function pair (fi, fj): flags 1 overlap, 2 kinetic,
+// 4 nuclear attraction (nuclei Z, Rn).  Returns false (status bit set) on unsupported
+// angular momentum.
+__device__ bool qb_onebody_pair(const GenBasis& b, int fi, int fj, int flags, int nnuc, const double* __restrict__ Z,
+                                const double* __restrict__ Rn, const double* __restrict__ boys, double& s_out,
+                                double& t_out, double& v_out, int* status) {
     double s_acc = 0.0, t_acc = 0.0, v_acc = 0.0;
     double ex[GEN_E_MAX], ey[GEN_E_MAX], ez[GEN_E_MAX], F[GEN_LTOT_ERI + 1];
     double r0[GEN_BOX_MAX], r1[GEN_BOX_MAX];
@@ -117,7 +113,7 @@ __global__ void qb_onebody_kernel(const GenBasis b, int flags, int nnuc, const d
             if (la[0] + lb[0] > 2 * GEN_LF_MAX || la[1] + lb[1] > 2 * GEN_LF_MAX ||
                 la[2] + lb[2] > 2 * GEN_LF_MAX) {
                 atomicOr(status, QB_DEVERR_BAD_INDEX);
-                return;
+                return false;
             }
             const double p = a + be, oo2p = 0.5 / p, mu = a * be / p;
             double P[3], PA[3], PB[3], AB2 = 0.0;
@@ -160,7 +156,7 @@ __global__ void qb_onebody_kernel(const GenBasis b, int flags, int nnuc, const d
                 const int Lt = nx + ny + nz - 3;
                 if (nx * ny * nz > GEN_BOX_MAX || Lt > GEN_LTOT_ERI) {
                     atomicOr(status, QB_DEVERR_BAD_INDEX);
-                    return;
+                    return false;
                 }
                 double vsum = 0.0;
                 for (int c = 0; c < nnuc; ++c) {
@@ -180,10 +176,109 @@ __global__ void qb_onebody_kernel(const GenBasis b, int flags, int nnuc, const d
             }
         }
     }
+    s_out = s_acc;
+    t_out = t_acc;
+    v_out = v_acc;
+    return true;
+}
+
+// One-electron matrices: one thread per function pair i >= j.
+// flags: 1 overlap, 2 kinetic, 4 nuclear attraction.  Outputs column-major, both triangles.
+__global__ void qb_onebody_kernel(const GenBasis b, int flags, int nnuc, const double* __restrict__ Z,
+                                  const double* __restrict__ Rn, const double* __restrict__ boys,
+                                  double* S, double* T, double* V, int* status) {
+    const long long npair = (long long)b.nfun * (b.nfun + 1) / 2;
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= npair) return;
+    int fi, fj;
+    tri_decode(n, fi, fj);
+    double s_acc, t_acc, v_acc;
+    if (!qb_onebody_pair(b, fi, fj, flags, nnuc, Z, Rn, boys, s_acc, t_acc, v_acc, status)) return;
     const size_t N = b.nfun;
     if (flags & 1) { S[fi + N * fj] = s_acc; S[fj + N * fi] = s_acc; }
     if (flags & 2) { T[fi + N * fj] = t_acc; T[fj + N * fi] = t_acc; }
     if (flags & 4) { V[fi + N * fj] = v_acc; V[fj + N * fi] = v_acc; }
+}
+
+// Batched overlap and core Hamiltonian of many molecules whose bases are concatenated
+// in b: molecule m owns functions [fo[m], fo[m] + nf[m]), nuclei [nuc0[m], nuc0[m+1]),
+// its function pairs are [poff[m], poff[m+1]) of the global pair index, and its
+// matrices start at S + mo[m], H + mo[m] (nf[m] x nf[m], column-major).
+__global__ void qb_onebody_batch_kernel(const GenBasis b, int nmol, const long long* __restrict__ poff,
+                                        const int* __restrict__ fo, const int* __restrict__ nf,
+                                        const long long* __restrict__ mo, const int* __restrict__ nuc0,
+                                        const double* __restrict__ Z, const double* __restrict__ Rn,
+                                        const double* __restrict__ boys, double* S, double* H, int* status) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= poff[nmol]) return;
+    int lo = 0, hi = nmol;   // poff[lo] <= g < poff[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (poff[mid] <= g) lo = mid; else hi = mid;
+    }
+    const int m = lo;
+    int i, j;
+    tri_decode(g - poff[m], i, j);
+    double s, t, v;
+    const int c0 = nuc0[m];
+    if (!qb_onebody_pair(b, fo[m] + i, fo[m] + j, 7, nuc0[m + 1] - c0, Z + c0, Rn + 3 * c0, boys, s, t, v, status))
+        return;
+    const size_t n = nf[m];
+    double* Sm = S + mo[m];
+    double* Hm = H + mo[m];
+    Sm[i + n * j] = s;
+    Sm[j + n * i] = s;
+    Hm[i + n * j] = t + v;
+    Hm[j + n * i] = t + v;
+}
+
+// Multipole-moment matrix M_ij = <i| prod_k (x_k - C_k)^{n_k} |j>: one thread per function
+// pair i >= j.  Per axis, (x - C)^n = sum_q binom(n, q) (B - C)^q (x - B)^{n-q} raises the
+// right primitive's power, and each term is a 1D overlap E^{i, j+n-q}_0 sqrt(pi/p).
+__global__ void qb_multipole_kernel(const GenBasis b, double Cx, double Cy, double Cz, int nx, int ny, int nz,
+                                    double* __restrict__ M, int* status) {
+    const long long npair = (long long)b.nfun * (b.nfun + 1) / 2;
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= npair) return;
+    int fi, fj;
+    tri_decode(n, fi, fj);
+    const double C[3] = {Cx, Cy, Cz};
+    const int deg[3] = {nx, ny, nz};
+    double acc = 0.0;
+    double e[GEN_E_MAX];
+    for (int pa = b.fp[fi]; pa < b.fp[fi + 1]; ++pa) {
+        for (int pb = b.fp[fj]; pb < b.fp[fj + 1]; ++pb) {
+            const double a = b.alpha[pa], be = b.alpha[pb];
+            const double* A = b.cen + 3 * pa;
+            const double* B = b.cen + 3 * pb;
+            const int* la = b.ijk + 3 * pa;
+            const int* lb = b.ijk + 3 * pb;
+            const double p = a + be, oo2p = 0.5 / p, mu = a * be / p;
+            const double sp = sqrt(QB_PI / p);
+            double AB2 = 0.0, prod = 1.0;
+            for (int k = 0; k < 3; ++k) {
+                const double Pk = (a * A[k] + be * B[k]) / p;
+                AB2 += (A[k] - B[k]) * (A[k] - B[k]);
+                if (la[k] + lb[k] + deg[k] > GEN_E_MAX - 1) {
+                    atomicOr(status, QB_DEVERR_BAD_INDEX);
+                    return;
+                }
+                const double BC = B[k] - C[k];
+                double sum = 0.0, pw = 1.0, binom = 1.0;
+                for (int q = 0; q <= deg[k]; ++q) {
+                    md_expand(la[k], lb[k] + deg[k] - q, Pk - A[k], Pk - B[k], oo2p, e);
+                    sum += binom * pw * e[0];
+                    pw *= BC;
+                    binom = binom * (deg[k] - q) / (q + 1);
+                }
+                prod *= sum * sp;
+            }
+            acc += exp(-mu * AB2) * b.w[pa] * b.w[pb] * prod;
+        }
+    }
+    const size_t N = b.nfun;
+    M[fi + N * fj] = acc;
+    M[fj + N * fi] = acc;
 }
 
 // Contracted ERI (ij|kl) of four functions by McMurchie–Davidson.
@@ -328,6 +423,28 @@ int qb_gen_onebody(const GenDevBasis& gb, int flags, int nnuc, const double* dZ,
     const int block = 64;
     const long long grid = (npair + block - 1) / block;
     if (grid > 0) qb_onebody_kernel<<<(unsigned)grid, block, 0, s>>>(b, flags, nnuc, dZ, dR, boys, S, T, V, status);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int qb_gen_onebody_batch(const GenDevBasis& gb, int nmol, long long npair_total, const long long* poff,
+                         const int* fo, const int* nf, const long long* mo, const int* nuc0, const double* dZ,
+                         const double* dR, const double* boys, double* S, double* H, int* status, cudaStream_t s) {
+    GenBasis b{gb.fp, gb.cen, gb.ijk, gb.alpha, gb.w, gb.nfun};
+    const int block = 64;
+    const long long grid = (npair_total + block - 1) / block;
+    if (grid > 0)
+        qb_onebody_batch_kernel<<<(unsigned)grid, block, 0, s>>>(b, nmol, poff, fo, nf, mo, nuc0, dZ, dR, boys, S, H,
+                                                                status);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int qb_gen_multipole(const GenDevBasis& gb, const double* C, const int* deg, double* M, int* status, cudaStream_t s) {
+    GenBasis b{gb.fp, gb.cen, gb.ijk, gb.alpha, gb.w, gb.nfun};
+    const long long npair = (long long)gb.nfun * (gb.nfun + 1) / 2;
+    const int block = 64;
+    const long long grid = (npair + block - 1) / block;
+    if (grid > 0)
+        qb_multipole_kernel<<<(unsigned)grid, block, 0, s>>>(b, C[0], C[1], C[2], deg[0], deg[1], deg[2], M, status);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

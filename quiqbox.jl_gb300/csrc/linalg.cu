@@ -2,6 +2,7 @@
 // the J/K finalisation and the DIIS coefficient solve.
 #include <cuda_runtime.h>
 #include "qb_internal.h"
+#include "qb_dense.cuh"
 
 // ---------------------------------------------------------------------------
 // C = alpha op(A) op(B) + beta C, column-major, 32x32 tiles in shared memory,
@@ -63,119 +64,9 @@ void qb_gemm(cudaStream_t s, int transA, int transB, int m, int n, int k, double
 #define QB_EIGH_MAXN 1024
 __global__ void __launch_bounds__(1024) qb_jacobi_kernel(int n, double* A, double* V, double* w, double* wtmp,
                                                          double* Vtmp, int* status) {
-    __shared__ double cs[QB_EIGH_MAXN / 2], sn[QB_EIGH_MAXN / 2];
-    __shared__ int pp[QB_EIGH_MAXN / 2], qq[QB_EIGH_MAXN / 2];
-    __shared__ int pos[QB_EIGH_MAXN];
-    __shared__ double red[32];
-    __shared__ int done;
-    const int tid = threadIdx.x, nt = blockDim.x;
-    const int m = n + (n & 1);
-    const int half = m / 2;
-    for (int i = tid; i < n * n; i += nt) V[i] = ((i % n) == (i / n)) ? 1.0 : 0.0;
-    if (tid == 0) done = 0;
-    __syncthreads();
-    for (int sweep = 0; sweep < 60; ++sweep) {
-        // convergence test
-        double off = 0.0, tot = 0.0;
-        for (int i = tid; i < n * n; i += nt) {
-            const double a = A[i];
-            tot += a * a;
-            if ((i % n) != (i / n)) off += a * a;
-        }
-        for (int d = 16; d > 0; d >>= 1) {
-            off += __shfl_down_sync(0xffffffffu, off, d);
-            tot += __shfl_down_sync(0xffffffffu, tot, d);
-        }
-        if ((tid & 31) == 0) { red[tid >> 5] = off; }
-        __syncthreads();
-        if (tid == 0) {
-            double o = 0.0;
-            for (int k = 0; k < (nt + 31) / 32; ++k) o += red[k];
-            red[31] = o;
-        }
-        __syncthreads();
-        const double offt = red[31];
-        __syncthreads();
-        if ((tid & 31) == 0) red[tid >> 5] = tot;
-        __syncthreads();
-        if (tid == 0) {
-            double t = 0.0;
-            for (int k = 0; k < (nt + 31) / 32; ++k) t += red[k];
-            done = (offt <= 1e-30 * t || offt == 0.0) ? 1 : 0;
-        }
-        __syncthreads();
-        if (done) break;
-        if (sweep == 59) {
-            if (tid == 0) atomicOr(status, 2);
-            break;
-        }
-        for (int i = tid; i < m; i += nt) pos[i] = i;
-        __syncthreads();
-        for (int round = 0; round < m - 1; ++round) {
-            for (int k = tid; k < half; k += nt) {
-                int p = pos[k], q = pos[m - 1 - k];
-                if (p > q) { const int t = p; p = q; q = t; }
-                double c = 1.0, s = 0.0;
-                if (q < n) {
-                    const double apq = A[p + (size_t)n * q];
-                    if (fabs(apq) > 1e-300) {
-                        const double theta = (A[q + (size_t)n * q] - A[p + (size_t)n * p]) / (2.0 * apq);
-                        const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-                        c = 1.0 / sqrt(t * t + 1.0);
-                        s = t * c;
-                    }
-                }
-                pp[k] = p; qq[k] = q; cs[k] = c; sn[k] = s;
-            }
-            __syncthreads();
-            // columns p, q of A and V
-            for (int idx = tid; idx < half * n; idx += nt) {
-                const int k = idx / n, r = idx % n;
-                const int p = pp[k], q = qq[k];
-                if (q >= n || sn[k] == 0.0) continue;
-                const double c = cs[k], s = sn[k];
-                const double ap = A[r + (size_t)n * p], aq = A[r + (size_t)n * q];
-                A[r + (size_t)n * p] = c * ap - s * aq;
-                A[r + (size_t)n * q] = s * ap + c * aq;
-                const double vp = V[r + (size_t)n * p], vq = V[r + (size_t)n * q];
-                V[r + (size_t)n * p] = c * vp - s * vq;
-                V[r + (size_t)n * q] = s * vp + c * vq;
-            }
-            __syncthreads();
-            // rows p, q of A
-            for (int idx = tid; idx < half * n; idx += nt) {
-                const int k = idx / n, col = idx % n;
-                const int p = pp[k], q = qq[k];
-                if (q >= n || sn[k] == 0.0) continue;
-                const double c = cs[k], s = sn[k];
-                const double ap = A[p + (size_t)n * col], aq = A[q + (size_t)n * col];
-                A[p + (size_t)n * col] = c * ap - s * aq;
-                A[q + (size_t)n * col] = s * ap + c * aq;
-            }
-            __syncthreads();
-            if (tid == 0) {   // rotate positions 1..m-1
-                const int last = pos[m - 1];
-                for (int i = m - 1; i > 1; --i) pos[i] = pos[i - 1];
-                pos[1] = last;
-            }
-            __syncthreads();
-        }
-    }
-    // ascending order (stable by index)
-    for (int i = tid; i < n; i += nt) wtmp[i] = A[i + (size_t)n * i];
-    __syncthreads();
-    for (int i = tid; i < n; i += nt) {
-        const double wi = wtmp[i];
-        int r = 0;
-        for (int j = 0; j < n; ++j) {
-            const double wj = wtmp[j];
-            r += (wj < wi) || (wj == wi && j < i);
-        }
-        w[r] = wi;
-        for (int row = 0; row < n; ++row) Vtmp[row + (size_t)n * r] = V[row + (size_t)n * i];
-    }
-    __syncthreads();
-    for (int i = tid; i < n * n; i += nt) V[i] = Vtmp[i];
+    __shared__ QbJacobiSmem<QB_EIGH_MAXN> sm;
+    const int used = qb_cta_jacobi<QB_EIGH_MAXN>(n, A, V, nullptr, w, wtmp, Vtmp, 59, sm);
+    if (used < 0 && threadIdx.x == 0) atomicOr(status, 2);
 }
 
 // w (n), V (n x n) from symmetric A; work needs 2 n^2 + n doubles.

@@ -22,6 +22,10 @@ struct GenDevBasis {
 };
 
 // generic.cu
+int qb_gen_onebody_batch(const GenDevBasis& gb, int nmol, long long npair_total, const long long* poff,
+                         const int* fo, const int* nf, const long long* mo, const int* nuc0, const double* dZ,
+                         const double* dR, const double* boys, double* S, double* H, int* status, cudaStream_t s);
+int qb_gen_multipole(const GenDevBasis& gb, const double* C, const int* deg, double* M, int* status, cudaStream_t s);
 int qb_gen_onebody(const GenDevBasis& gb, int flags, int nnuc, const double* dZ, const double* dR,
                    const double* boys, double* S, double* T, double* V, int* status, cudaStream_t s);
 int qb_gen_eri(const GenDevBasis& gb, int mode, const double* boys, double* eri, const double* D, double* Jp,
@@ -69,6 +73,17 @@ struct HostShell {
     int prim0;   // into the shell-primitive arrays (alpha, coef)
     int f0;      // first function
 };
+
+// Primitive-pair slot: shells and shell-primitive indices (into the flattened basis).
+struct PairSlot {
+    int sa, sb, pa, pb;
+};
+int qb_build_prim_pairs(cudaStream_t s, const PairSlot* d_slots, int nslot, const double* d_cen,
+                        const double* d_alpha, const double* d_w, const ShellPair* d_pairs, int npair,
+                        PrimPair* d_prims, float4* d_prims32, int* d_nkept, unsigned long long* d_kmax);
+
+bool qb_detect_shells(int f_begin, int f_end, const int* fp, const double* cen, const int* ijk, const double* al,
+                      const double* w, std::vector<HostShell>& shells, double* ratio);
 
 struct qb_ctx {
     int device = 0;

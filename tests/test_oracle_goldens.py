@@ -212,3 +212,29 @@ def test_boys_at_x_equal_order_one(oracle):
     ref = float(mpmath.quad(lambda t: t ** 2 * mpmath.exp(-t * t), [0, 1]))
     assert oracle.boys(1.0, 1) == pytest.approx(ref, rel=1e-14)
     assert oracle.boys_exact(1.0, 1) == pytest.approx(ref, rel=1e-15)
+
+
+def _interface_orbs(qb):
+    # Interface-test.jl:7-18,39: cgf1, cgf2 (p_x contractions) and cgf3 = cgf1 with (3, 0, 0)
+    cen1, cen2 = (1.1, 0.5, 1.1), (1.0, 1.5, 1.1)
+    cgf1 = qb.genGaussTypeOrb(cen1, [1.2, 0.6], [1.5, -0.3], (1, 0, 0))
+    cgf2 = qb.genGaussTypeOrb(cen2, [1.5, 0.6], [1.0, 0.8], (1, 0, 0))
+    cgf3 = qb.genGaussTypeOrb(cen1, [1.2, 0.6], [1.5, -0.3], (3, 0, 0))
+    return cen1, cgf1, cgf2, cgf3
+
+
+def test_multipole_identities(qb, oracle):
+    # Interface-test.jl:38-44: degree 0 is the overlap; x^2 about cgf1's centre turns cgf1
+    # into cgf3, so <cgf2|(x-C1)^2|cgf1> = <cgf2|cgf3> (and the transposed order agrees)
+    cen1, cgf1, cgf2, cgf3 = _interface_orbs(qb)
+    fb = qb.flatten([cgf1, cgf2, cgf3])
+    S = oracle.overlaps(fb)
+    M0 = oracle.multipoles(fb, cen1, (0, 0, 0))
+    assert M0[0, 1] == S[0, 1]
+    M2 = oracle.multipoles(fb, cen1, (2, 0, 0))
+    assert M2[1, 0] == pytest.approx(S[1, 2], rel=1e-14)
+    assert M2[0, 1] == pytest.approx(S[1, 2], rel=1e-14)
+    # quad precision agrees with the Float64 restatement
+    Mq = oracle.multipoles(fb, (1.0, 0.0, 0.0), (2, 2, 2), exact=True)
+    Md = oracle.multipoles(fb, (1.0, 0.0, 0.0), (2, 2, 2))
+    assert np.abs(Mq - Md).max() < 1e-13 * max(1.0, np.abs(Mq).max())
