@@ -160,6 +160,42 @@ void qb_scf_config_default(qb_scf_config* cfg);
 int qb_run_hartree_fock(qb_ctx* ctx, const qb_basis* basis, int nnuc, const double* Z, const double* R,
                         int n_alpha, int n_beta, const qb_scf_config* cfg, qb_scf_result* res);
 
+/* Batched closed-shell Hartree–Fock over many independent molecules in one call.
+ * The reference solves one molecule per runHartreeFock (src/HartreeFock.jl:953-1046);
+ * this runs hundreds of them together: integrals of all molecules once (screened ERI
+ * blocks stored on the device), then CUDA-graph-captured SCF iterations, each one batched
+ * launch per step for every molecule not yet converged.  Per molecule: a flattened basis
+ * of s and p Cartesian shells (1 <= nfun <= 256), nnuc[m] nuclei (charges and positions
+ * concatenated over molecules in Z and R), nocc[m] doubly occupied orbitals.  Core-
+ * Hamiltonian guess, symmetric orthogonalisation, Pulay DIIS; converged when
+ * |dE| <= conv_energy and RMS(dD_total) <= conv_density.  energy[m] receives the
+ * electronic energy (add the nuclear repulsion for the total). */
+typedef struct {
+    double conv_energy;     /* default 1e-10 Ha */
+    double conv_density;    /* default 1e-8 */
+    int max_iter;           /* default 200 */
+    int diis_size;          /* 1..15, default 15 (1 = no extrapolation) */
+    double schwarz;         /* stored-integral screening Q_ab Q_cd >= schwarz, default 1e-14 */
+    int iters_per_graph;    /* SCF iterations per CUDA-graph launch, default 4 */
+} qb_batch_config;
+
+typedef struct {
+    double* energy;         /* nmol electronic energies (caller-allocated, may be NULL) */
+    int* iterations;        /* nmol */
+    int* converged;         /* nmol: 1 if converged */
+    int* jacobi_sweeps;     /* nmol: Jacobi sweeps summed over the iterations */
+    double ms_integrals;    /* device time: one-body, pairs, Schwarz, stored ERIs, orthogonalisation */
+    double ms_scf;          /* device time of the SCF iterations */
+    int64_t quartets;       /* stored shell quartets */
+    int64_t prim_quartets;  /* primitive quartets evaluated for them */
+    int64_t eri_doubles;    /* stored integrals */
+    int graph_launches;
+} qb_batch_result;
+
+void qb_batch_config_default(qb_batch_config* cfg);
+int qb_run_rhf_batched(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nnuc, const double* Z,
+                       const double* R, const int* nocc, const qb_batch_config* cfg, qb_batch_result* res);
+
 /* Measured FP64 FMA throughput of this device (TFLOP/s), the FP64 roofline denominator. */
 int qb_fp64_peak(qb_ctx* ctx, double* tflops);
 
@@ -172,7 +208,7 @@ int qb_fp64_peak(qb_ctx* ctx, double* tflops);
  * alpha, weight), dD is the nfun x nfun density, dJ / dK receive the results;
  * `stream` is a cudaStream_t (NULL = legacy default stream).  No Schwarz screening.
  *  - Limit: nfun <= 512; larger bases return QB_ERR_DIM before touching any pointer.
- * *  - Scratch: a file-scope device array of 4 MiB (+ a 2.1 MiB Boys table) held by
+ *  - Scratch: a file-scope device array of 4 MiB (+ a 2.1 MiB Boys table) held by
  *    every GPU that loads the library until exit.  The first call on a device does
  *    the set-up (resolves the arrays' device addresses, uploads the Boys table) and
  *    must come before any stream capture on that device.

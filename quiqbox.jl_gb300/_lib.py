@@ -20,7 +20,8 @@ QB_OK, QB_ERR_ARG, QB_ERR_DIM, QB_ERR_DOMAIN, QB_ERR_CUDA, QB_ERR_TIMEOUT, QB_ER
 EXPORTED = ["qb_create", "qb_destroy", "qb_last_error", "qb_device_info", "qb_overlaps", "qb_elec_kinetics",
             "qb_nuc_attractions", "qb_core_hamiltonian", "qb_elec_repulsions", "qb_elec_repulsion_list", "qb_jk",
             "qb_jk_prepare", "qb_jk_upload_density", "qb_jk_execute", "qb_jk_download", "qb_jk_get_stats", "qb_jk_pair_table",
-            "qb_scf_config_default", "qb_run_hartree_fock", "qb_fp64_peak", "qb_jk_noalloc", "qb_boys", "qb_multipole_moments"]
+            "qb_scf_config_default", "qb_run_hartree_fock", "qb_fp64_peak", "qb_jk_noalloc", "qb_boys", "qb_multipole_moments",
+            "qb_batch_config_default", "qb_run_rhf_batched"]
 
 
 class DimensionMismatch(ValueError):
@@ -106,7 +107,7 @@ def load():
         L.qb_jk_noalloc.argtypes = [pb, vp, vp, vp, vp]
         for name in EXPORTED:
             f = getattr(L, name)
-            if name not in ("qb_destroy", "qb_last_error", "qb_scf_config_default"):
+            if name not in ("qb_destroy", "qb_last_error", "qb_scf_config_default", "qb_batch_config_default"):
                 f.restype = C.c_int
         _lib = L
         return L
@@ -158,6 +159,18 @@ class Context:
         if rc == QB_ERR_UNSUPPORTED:
             raise NotImplementedError(msg)
         raise QBError(f"status {rc}: {msg}")
+
+
+class QBBatchConfig(C.Structure):
+    _fields_ = [("conv_energy", C.c_double), ("conv_density", C.c_double), ("max_iter", C.c_int),
+                ("diis_size", C.c_int), ("schwarz", C.c_double), ("iters_per_graph", C.c_int)]
+
+
+class QBBatchResult(C.Structure):
+    _fields_ = [("energy", C.POINTER(C.c_double)), ("iterations", C.POINTER(C.c_int)),
+                ("converged", C.POINTER(C.c_int)), ("jacobi_sweeps", C.POINTER(C.c_int)),
+                ("ms_integrals", C.c_double), ("ms_scf", C.c_double), ("quartets", C.c_int64),
+                ("prim_quartets", C.c_int64), ("eri_doubles", C.c_int64), ("graph_launches", C.c_int)]
 
 
 class BasisArgs:

@@ -316,6 +316,78 @@ def computeBoysFunc(T, m, ctx=None):
     return float(computeBoysSequence(np.array([T]), m, path=1 if m > 8 else 0, ctx=ctx)[0, m])
 
 
+@dataclass
+class BatchSCFConfig:
+    """Configuration of runHartreeFockBatched (qb_batch_config)."""
+    conv_energy: float = 1e-10
+    conv_density: float = 1e-8
+    max_iter: int = 200
+    diis_size: int = 15
+    schwarz: float = 1e-14
+    iters_per_graph: int = 4
+
+
+@dataclass
+class BatchSCFResult:
+    energies: np.ndarray          # total energies (electronic + nuclear repulsion), Ha
+    elec_energies: np.ndarray
+    iterations: np.ndarray
+    converged: np.ndarray
+    jacobi_sweeps: np.ndarray
+    nfun: np.ndarray
+    ms_integrals: float
+    ms_scf: float
+    quartets: int
+    prim_quartets: int
+    eri_doubles: int
+    graph_launches: int
+
+
+def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ctx=None) -> BatchSCFResult:
+    """Closed-shell HF of many molecules in one call (qb_run_rhf_batched).
+
+    molecules: sequence of (nucInfo, basis) or (nucInfo, basis, charge); nucInfo a
+    NuclearCluster, basis a list of orbitals or a FlatBasis.  Each molecule is what
+    runHartreeFock (HartreeFock.jl:972-1046) would solve with initial=:CoreH and the
+    :DIIS method, all of them sharing every launch."""
+    c = _ctx(ctx)
+    cfg = config or BatchSCFConfig()
+    nmol = len(molecules)
+    args, nnuc, Zs, Rs, nocc, enn, nf = [], [], [], [], [], [], []
+    for mol in molecules:
+        nuc, basis = mol[0], mol[1]
+        charge = mol[2] if len(mol) > 2 else 0
+        fb = _flat(basis)
+        Zm = nuc.charges
+        nel = int(round(Zm.sum())) - int(charge)
+        if nel <= 0 or nel % 2:
+            raise DomainError("closed-shell molecule needs a positive even electron count")
+        args.append(L.BasisArgs(fb))
+        nnuc.append(len(Zm))
+        Zs.append(Zm)
+        Rs.append(nuc.positions.reshape(-1))
+        nocc.append(nel // 2)
+        enn.append(nucRepulsion(nuc))
+        nf.append(fb.nfun)
+    bases = (L.QBBasis * nmol)(*[a.s for a in args])
+    nnuc_a = np.ascontiguousarray(nnuc, np.int32)
+    Z = np.ascontiguousarray(np.concatenate(Zs), np.float64)
+    R = np.ascontiguousarray(np.concatenate(Rs), np.float64)
+    nocc_a = np.ascontiguousarray(nocc, np.int32)
+    qcfg = L.QBBatchConfig(cfg.conv_energy, cfg.conv_density, cfg.max_iter, cfg.diis_size, cfg.schwarz,
+                           cfg.iters_per_graph)
+    E = np.zeros(nmol)
+    it = np.zeros(nmol, np.int32)
+    conv = np.zeros(nmol, np.int32)
+    sw = np.zeros(nmol, np.int32)
+    res = L.QBBatchResult(L.dptr(E), L.iptr(it), L.iptr(conv), L.iptr(sw), 0.0, 0.0, 0, 0, 0, 0)
+    c.check(c.lib.qb_run_rhf_batched(c.h, nmol, bases, L.iptr(nnuc_a), L.dptr(Z), L.dptr(R), L.iptr(nocc_a),
+                                     C.byref(qcfg), C.byref(res)))
+    return BatchSCFResult(E + np.array(enn), E, it, conv.astype(bool), sw, np.array(nf), res.ms_integrals,
+                          res.ms_scf, int(res.quartets), int(res.prim_quartets), int(res.eri_doubles),
+                          int(res.graph_launches))
+
+
 def fp64_peak(ctx=None):
     """Measured FP64 FMA throughput of the device (TFLOP/s)."""
     c = _ctx(ctx)

@@ -217,6 +217,12 @@ int qb_boys(qb_ctx* ctx, int n, const double* T, int M, int path, double* F) {
     return QB_OK;
 }
 
+int qb_run_rhf_batched(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nnuc, const double* Z,
+                       const double* R, const int* nocc, const qb_batch_config* cfg, qb_batch_result* res) {
+    QB_TRY(enter(ctx));
+    return qb_batch_rhf_run(ctx, nmol, bases, nnuc, Z, R, nocc, cfg, res);
+}
+
 int qb_jk_prepare(qb_ctx* ctx, const qb_basis* basis, double schwarz) {
     QB_TRY(enter(ctx));
     if (!(schwarz >= 0.0)) return qb_set_error(ctx, QB_ERR_DOMAIN, "Schwarz threshold must be >= 0");

@@ -23,8 +23,8 @@ __device__ __forceinline__ double qb_cta_sum(double v, double* red) {
 
 // C = alpha op(A) op(B) + beta C, op(A) m x k, op(B) k x n.  beta == 0 ignores C's contents.
 // Ends with a block barrier.
-__device__ void qb_cta_gemm(bool tA, bool tB, int m, int n, int k, double alpha, const double* A, int lda,
-                            const double* B, int ldb, double beta, double* C, int ldc) {
+static __device__ void qb_cta_gemm(bool tA, bool tB, int m, int n, int k, double alpha, const double* A, int lda,
+                                   const double* B, int ldb, double beta, double* C, int ldc) {
     for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) {
         const int i = idx % m, j = idx / m;
         double s = 0.0;
@@ -49,7 +49,7 @@ struct QbJacobiSmem {
     int pp[MAXN / 2], qq[MAXN / 2];
     int pos[MAXN];
     double red[33];
-    int done;
+    int rotated;
 };
 
 // Eigen-decomposition of the symmetric n x n matrix A (destroyed) by the cyclic Jacobi
@@ -57,8 +57,12 @@ struct QbJacobiSmem {
 // planes).  V (n x n) receives the eigenvectors in columns, w the eigenvalues, both
 // in ascending order; wtmp (n) and Vtmp (n x n) are scratch.  If Vin is non-null the
 // rotations are applied to a copy of Vin instead of the identity (V = Vin * rotations:
-// eigenvectors of Vin A Vin^T for orthogonal Vin).  At most maxsweep sweeps; returns
-// the number used, or -1 if off(A)^2 > 1e-30 ||A||^2 after the last.
+// eigenvectors of Vin A Vin^T for orthogonal Vin).  A plane (p, q) is rotated only while
+// |a_pq| > 1e-15 sqrt(|a_pp a_qq|) (below that the rotation changes nothing at double
+// precision); converged when off(A)^2 <= 1e-30 ||A||^2, when a sweep rotated no plane, or
+// when off(A)^2 <= 1e-24 ||A||^2 stopped shrinking (rounding level: it fell by less than
+// 4x in the last sweep).  At most maxsweep sweeps; returns the number used, or -1 if not
+// converged (off(A) is then still reported small enough by the caller's own test).
 template <int MAXN>
 __device__ int qb_cta_jacobi(int n, double* A, double* V, const double* Vin, double* w, double* wtmp, double* Vtmp,
                              int maxsweep, QbJacobiSmem<MAXN>& sm) {
@@ -68,6 +72,7 @@ __device__ int qb_cta_jacobi(int n, double* A, double* V, const double* Vin, dou
     for (int i = tid; i < n * n; i += nt) V[i] = Vin ? Vin[i] : (((i % n) == (i / n)) ? 1.0 : 0.0);
     __syncthreads();
     int used = -1;
+    double off_prev = 0.0;
     for (int sweep = 0; sweep <= maxsweep; ++sweep) {
         double off = 0.0, tot = 0.0;
         for (int i = tid; i < n * n; i += nt) {
@@ -77,12 +82,15 @@ __device__ int qb_cta_jacobi(int n, double* A, double* V, const double* Vin, dou
         }
         off = qb_cta_sum(off, sm.red);
         tot = qb_cta_sum(tot, sm.red);
-        if (off <= 1e-30 * tot || off == 0.0) {
+        if (off <= 1e-30 * tot || off == 0.0 || (sweep > 0 && sm.rotated == 0) ||
+            (sweep > 0 && off <= 1e-24 * tot && off > 0.25 * off_prev)) {
             used = sweep;
             break;
         }
+        off_prev = off;
         if (sweep == maxsweep) break;
         for (int i = tid; i < m; i += nt) sm.pos[i] = i;
+        if (tid == 0) sm.rotated = 0;
         __syncthreads();
         for (int round = 0; round < m - 1; ++round) {
             for (int k = tid; k < half; k += nt) {
@@ -91,11 +99,13 @@ __device__ int qb_cta_jacobi(int n, double* A, double* V, const double* Vin, dou
                 double c = 1.0, s = 0.0;
                 if (q < n) {
                     const double apq = A[p + (size_t)n * q];
-                    if (fabs(apq) > 1e-300) {
-                        const double theta = (A[q + (size_t)n * q] - A[p + (size_t)n * p]) / (2.0 * apq);
+                    const double app = A[p + (size_t)n * p], aqq = A[q + (size_t)n * q];
+                    if (fabs(apq) > 1e-300 && fabs(apq) > 1e-15 * sqrt(fabs(app * aqq))) {
+                        const double theta = (aqq - app) / (2.0 * apq);
                         const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
                         c = 1.0 / sqrt(t * t + 1.0);
                         s = t * c;
+                        sm.rotated = 1;
                     }
                 }
                 sm.pp[k] = p; sm.qq[k] = q; sm.cs[k] = c; sm.sn[k] = s;

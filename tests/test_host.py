@@ -61,3 +61,30 @@ def test_workload_generator_shapes(qb):
     assert d.min() >= 1.3 and c.min() >= 0 and c.max() <= 14
     D = random_density(20)
     assert np.allclose(D, D.T) and np.linalg.eigvalsh(D).min() > -1e-12
+
+
+def test_batch_molecule_generator():
+    # batched-SCF workload: 2-16 atoms, H:C:N:O = 5:3:1:1, bonded chains with bonds in
+    # [1.8, 2.9] bohr and angles in [95, 130] degrees, STO-3G or 6-31G, even electrons
+    import numpy as np
+    import __graft_entry__ as ge
+    qb = ge.load_package()
+    from quiqbox_gb300.workloads import batch_molecules, _chain_positions
+    mols = batch_molecules(64, seed=0)
+    assert len(mols) == 64
+    for m in mols:
+        assert 2 <= len(m["symbols"]) <= 16
+        assert m["basis"] in ("STO-3G", "6-31G")
+        z = int(round(m["nuc"].charges.sum()))
+        assert (z - m["charge"]) % 2 == 0 and m["charge"] in (0, 1)
+        assert 1 <= m["flat"].nfun <= 144
+    again = batch_molecules(64, seed=0)
+    assert all(a["coords"] == b["coords"] and a["basis"] == b["basis"] for a, b in zip(mols, again))
+    rng = np.random.default_rng(1)
+    P = _chain_positions(10, rng)
+    d = np.linalg.norm(P[1:] - P[:-1], axis=1)
+    assert (d >= 1.8).all() and (d <= 2.9).all()
+    for k in range(1, 9):
+        u, v = P[k - 1] - P[k], P[k + 1] - P[k]
+        ang = np.degrees(np.arccos(u @ v / np.linalg.norm(u) / np.linalg.norm(v)))
+        assert 95.0 - 1e-9 <= ang <= 130.0 + 1e-9
