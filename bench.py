@@ -309,6 +309,11 @@ def run_ours(args):
     Jp = torch.empty(n * n, dtype=torch.float64, pin_memory=True).numpy()
     Kp = torch.empty(n * n, dtype=torch.float64, pin_memory=True).numpy()
     ctx.check(lib.qb_jk_upload_density(ctx.h, L.dptr(Dp)))
+    # per-class kernel variant chosen by timing on this workload (autotuned quartet kernels)
+    chosen = np.zeros(32, np.int32)
+    t_tune = time.perf_counter()
+    ctx.check(lib.qb_jk_autotune(ctx.h, 1, L.iptr(chosen)))
+    t_tune = time.perf_counter() - t_tune
     stats = L.QBJKStats()
     for _ in range(args.warmup):
         ctx.check(lib.qb_jk_execute(ctx.h))
@@ -365,7 +370,10 @@ def run_ours(args):
                        "schwarz": args.schwarz, "quartets": q, "prim_quartets": int(stats.prim_quartets),
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "flushed (256 MiB write) before every timed step",
-                       "wall_s_timed_region": wall, "jk_symmetry_rel": sym},
+                       "wall_s_timed_region": wall, "jk_symmetry_rel": sym,
+                       "autotune_s": t_tune,
+                       "kernel_variants": {"".join(str(v) for v in stats.class_l[c]): int(chosen[c])
+                                           for c in range(stats.nclass)}},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": None,
                          "peak_source": "measured: FP64 FMA microbenchmark (qb_fp64_peak) in this run",

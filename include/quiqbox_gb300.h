@@ -74,6 +74,14 @@ int qb_core_hamiltonian(qb_ctx* ctx, const qb_basis* basis, int nnuc, const doub
 int qb_multipole_moments(qb_ctx* ctx, const qb_basis* basis, const double center[3], const int degrees[3],
                          double* M);
 
+/* Autotuner of the direct J/K build (no counterpart in the reference): on the basis of the
+ * last qb_jk_prepare and the uploaded density, times every compiled kernel variant of
+ * every angular-momentum class on its actual quartet work list (best of `repeats`) and
+ * keeps the fastest per class for this context; variants[c] (nclass entries of
+ * qb_jk_stats, may be NULL) receives the choice (0: one quartet per thread, 1-3: warp-
+ * cooperative configurations).  Costs a few J/K builds; J and K stay those of the density. */
+int qb_jk_autotune(qb_ctx* ctx, int repeats, int* variants);
+
 /* Boys function sequence on the device: F[i*(M+1) + m] = F_m(T[i]), m = 0..M, T[i] >= 0.
  * Replaces computeBoysSequence (src/Integration/Engines/BoysFunction.jl:67-77) and
  * computeBoysFunc (:62-64).  path 0: the evaluator of the ERI class kernels (M <= 8);

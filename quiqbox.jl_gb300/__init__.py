@@ -13,6 +13,6 @@ from .api import (overlaps, overlap, elecKinetics, elecKinetic, nucAttractions, 
                   coreHamiltonian, elecRepulsions, elecRepulsion, elecRepulsion_list, jk, SCFconfig,
                   HFconfig, HFfinalInfo, runHartreeFock, RCHartreeFock, UOHartreeFock, fp64_peak, device_info,
                   computeBoysSequence, computeBoysFunc, multipoleMoments, multipoleMoment,
-                  runHartreeFockBatched, BatchSCFConfig, BatchSCFResult,
+                  runHartreeFockBatched, BatchSCFConfig, BatchSCFResult, jk_autotune,
                   DimensionMismatch, DomainError)
 from ._lib import Context, load as load_library, LIB_PATH, EXPORTED  # noqa: F401

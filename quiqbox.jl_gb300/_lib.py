@@ -21,7 +21,7 @@ EXPORTED = ["qb_create", "qb_destroy", "qb_last_error", "qb_device_info", "qb_ov
             "qb_nuc_attractions", "qb_core_hamiltonian", "qb_elec_repulsions", "qb_elec_repulsion_list", "qb_jk",
             "qb_jk_prepare", "qb_jk_upload_density", "qb_jk_execute", "qb_jk_download", "qb_jk_get_stats", "qb_jk_pair_table",
             "qb_scf_config_default", "qb_run_hartree_fock", "qb_fp64_peak", "qb_jk_noalloc", "qb_boys", "qb_multipole_moments",
-            "qb_batch_config_default", "qb_run_rhf_batched"]
+            "qb_batch_config_default", "qb_run_rhf_batched", "qb_jk_autotune"]
 
 
 class DimensionMismatch(ValueError):

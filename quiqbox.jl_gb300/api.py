@@ -297,6 +297,23 @@ def runHartreeFock(nucInfo, basis, config: Optional[HFconfig] = None, spin=None,
                        res.steps, (na, nb))
 
 
+def jk_autotune(basis, D, schwarz=1e-12, repeats=1, ctx=None):
+    """Times every compiled kernel variant of every angular-momentum class of the direct
+    J/K build on this basis and density and keeps the fastest per class in the context
+    (qb_jk_autotune).  Returns {class "la lb lc ld": variant}."""
+    c = _ctx(ctx)
+    fb = _flat(basis)
+    b = L.BasisArgs(fb)
+    Df = np.ascontiguousarray(np.asarray(D, dtype=np.float64).reshape(-1, order="F"))
+    c.check(c.lib.qb_jk_prepare(c.h, b.ref(), C.c_double(schwarz)))
+    c.check(c.lib.qb_jk_upload_density(c.h, L.dptr(Df)))
+    chosen = np.zeros(32, np.int32)
+    c.check(c.lib.qb_jk_autotune(c.h, int(repeats), L.iptr(chosen)))
+    st = L.QBJKStats()
+    c.check(c.lib.qb_jk_get_stats(c.h, C.byref(st)))
+    return {"".join(str(v) for v in st.class_l[k]): int(chosen[k]) for k in range(st.nclass)}
+
+
 def computeBoysSequence(T, M, path=0, ctx=None):
     """F_0..F_M at every T (array of shape T.shape + (M+1,)), evaluated on the device.
 

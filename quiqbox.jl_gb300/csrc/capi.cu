@@ -255,6 +255,11 @@ int qb_jk_execute(qb_ctx* ctx) {
     return QB_OK;
 }
 
+int qb_jk_autotune(qb_ctx* ctx, int repeats, int* variants) {
+    QB_TRY(enter(ctx));
+    return qb_jk_autotune_device(ctx, repeats, variants);
+}
+
 int qb_jk_download(qb_ctx* ctx, double* J, double* K) {
     QB_TRY(enter(ctx));
     if (!ctx->jk_prepared) return qb_set_error(ctx, QB_ERR_ARG, "call qb_jk_prepare first");

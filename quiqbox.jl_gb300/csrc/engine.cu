@@ -561,6 +561,60 @@ int qb_jk_device(qb_ctx* ctx, const double* dD, double* dJ, double* dK, double t
     return qb_cuda_check(ctx, cudaGetLastError(), "J/K finalize");
 }
 
+// Autotuner: after one J/K build on the current basis and density (work lists in place),
+// time every compiled kernel variant of every class with work on the same list (CUDA events
+// on the context stream, best of `repeats`) and keep the fastest per class.
+int qb_jk_autotune_device(qb_ctx* ctx, int repeats, int* chosen) {
+    if (!ctx->jk_prepared) return qb_set_error(ctx, QB_ERR_ARG, "call qb_jk_prepare first");
+    cudaStream_t s = ctx->stream;
+    QB_TRY(qb_jk_device(ctx, ctx->d_D.p, ctx->d_J.p, ctx->d_K.p, ctx->schwarz, s));
+    QB_CUDA(ctx, cudaStreamSynchronize(s));
+    if (!ctx->shell_path) return QB_OK;
+    const int n = ctx->nfun;
+    for (int c = 0; c < ctx->nclass; ++c) {
+        const ClassLaunchers& L = ctx->launch[c];
+        const int X = ctx->class_bra[c], Y = ctx->class_ket[c];
+        const int nbra = ctx->pc_off[X + 1] - ctx->pc_off[X], nket = ctx->pc_off[Y + 1] - ctx->pc_off[Y];
+        if (chosen) chosen[c] = ctx->variant[c];
+        if (nbra == 0 || nket == 0) continue;
+        int nvar = 0;
+        for (int v = 0; v < QB_NVARIANT; ++v) nvar += L.jk[v] != nullptr;
+        if (nvar < 2) continue;
+        const ClassWork w{ctx->d_pairs.p + ctx->pc_off[X], ctx->d_pairs.p + ctx->pc_off[Y],
+                          ctx->d_offs.p + ctx->offs_off[c], nbra, X == Y};
+        const JKArgs args{ctx->d_prims.p, ctx->d_prims32.p, ctx->boys.p, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p,
+                          ctx->d_primcount.p + c, n};
+        float best = 0.f;
+        int best_v = ctx->variant[c], best_occ = ctx->occ[c];
+        for (int v = 0; v < QB_NVARIANT; ++v) {
+            if (!L.jk[v]) continue;
+            const int occ = L.occupancy[v]();
+            const int grid = ctx->nsm * std::max(1, occ);
+            float t = 0.f;
+            for (int r = 0; r < std::max(1, repeats); ++r) {
+                QB_CUDA(ctx, cudaEventRecord(ctx->ev_start, s));
+                L.jk[v](w, args, grid, s);
+                QB_CUDA(ctx, cudaEventRecord(ctx->ev_stop, s));
+                QB_CUDA(ctx, cudaEventSynchronize(ctx->ev_stop));
+                float ms = 0.f;
+                QB_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+                t = (r == 0) ? ms : std::min(t, ms);
+            }
+            if (best == 0.f || t < best) {
+                best = t;
+                best_v = v;
+                best_occ = occ;
+            }
+        }
+        ctx->variant[c] = best_v;
+        ctx->occ[c] = best_occ;
+        if (chosen) chosen[c] = best_v;
+    }
+    QB_CUDA(ctx, cudaGetLastError());
+    // the timing runs accumulated into J'/K': leave the context's J and K consistent
+    return qb_jk_device(ctx, ctx->d_D.p, ctx->d_J.p, ctx->d_K.p, ctx->schwarz, s);
+}
+
 int qb_onebody_device(qb_ctx* ctx, int flags, int nnuc, const double* Z, const double* R, double* dS, double* dT,
                       double* dV) {
     cudaStream_t s = ctx->stream;

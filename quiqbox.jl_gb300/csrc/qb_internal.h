@@ -82,6 +82,7 @@ int qb_build_prim_pairs(cudaStream_t s, const PairSlot* d_slots, int nslot, cons
                         const double* d_alpha, const double* d_w, const ShellPair* d_pairs, int npair,
                         PrimPair* d_prims, float4* d_prims32, int* d_nkept, unsigned long long* d_kmax);
 
+int qb_jk_autotune_device(qb_ctx* ctx, int repeats, int* chosen);
 int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nnuc, const double* Z,
                      const double* R, const int* nocc, const qb_batch_config* cfg, qb_batch_result* res);
 

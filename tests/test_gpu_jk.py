@@ -135,3 +135,16 @@ def test_jk_kernel_variants(qb, oracle, tmp_path, variant):
         scale = max(np.abs(Jr).max(), 1.0)
         assert np.abs(got[tag + "_J"] - Jr).max() < tol * scale, tag
         assert np.abs(got[tag + "_K"] - Kr).max() < tol * scale, tag
+
+
+def test_jk_autotune_keeps_results(qb, oracle):
+    # the autotuner picks a kernel variant per class by timing; J and K stay exact
+    fb, D = _small_shell_system(qb, 0, n_h=2, n_heavy=1, box=4.0)
+    ctx = qb.Context(0)
+    chosen = qb.jk_autotune(fb, D, schwarz=0.0, ctx=ctx)
+    assert len(chosen) == 21 and all(0 <= v <= 3 for v in chosen.values())
+    J, K = qb.jk(fb, D, schwarz=0.0, ctx=ctx)
+    Jr, Kr = oracle.jk(fb, D, exact=True)
+    scale = max(np.abs(Jr).max(), 1.0)
+    assert np.abs(J - Jr).max() < 1e-12 * scale
+    assert np.abs(K - Kr).max() < 1e-12 * scale
