@@ -82,6 +82,31 @@ int qb_multipole_moments(qb_ctx* ctx, const qb_basis* basis, const double center
  * cooperative configurations).  Costs a few J/K builds; J and K stay those of the density. */
 int qb_jk_autotune(qb_ctx* ctx, int repeats, int* variants);
 
+/* Kernels of the learned initial guess (no counterpart in the reference): a small MLP
+ * with BF16 weights and activations and FP32 accumulation, trained and evaluated on the
+ * GPU (quiqbox.jl_gb300/guess.py builds the passes from these).  Device pointers; stream
+ * is a cudaStream_t.  Matrices are row-major.
+ * qb_bf16_gemm_nt: C (M x N, fp32) = A (M x K, bf16) * B^T (B: N x K, bf16) [+ bias (N)],
+ *   tensor cores (mma.sync BF16 -> FP32); M and N multiples of 64, K of 32, A and B
+ *   16-byte aligned.
+ * qb_gelu_forward: a (bf16) = GELU(z); qb_gelu_backward: dz = da * GELU'(z).
+ * qb_f32_to_bf16: y = bf16(x) (rows x cols) or its transpose (transpose != 0).
+ * qb_bf16_transpose: y (cols x rows) = x^T.
+ * qb_colsum: out[j] = sum_i x[i][j] (bias gradients).
+ * qb_mse_grad: dy = 2 w (y - t) / wsum and *loss += sum w (y - t)^2 / wsum.
+ * qb_adam_step: Adam (bias-corrected, step >= 1) on FP32 weights w with moments m, v;
+ *   refreshes the BF16 copy w_bf16 when non-NULL. */
+int qb_bf16_gemm_nt(int M, int N, int K, const void* A, const void* B, const float* bias, float* C, void* stream);
+int qb_gelu_forward(int64_t n, const float* z, void* a, void* stream);
+int qb_gelu_backward(int64_t n, const float* z, const float* da, float* dz, void* stream);
+int qb_f32_to_bf16(int rows, int cols, const float* x, void* y, int transpose, void* stream);
+int qb_bf16_transpose(int rows, int cols, const void* x, void* y, void* stream);
+int qb_colsum(int rows, int cols, const float* x, float* out, void* stream);
+int qb_mse_grad(int64_t n, const float* y, const float* t, const float* w, float wsum, float* dy, float* loss,
+                void* stream);
+int qb_adam_step(int64_t n, float* w, const float* g, float* m, float* v, void* w_bf16, float lr, float b1, float b2,
+                 float eps, int step, void* stream);
+
 /* Boys function sequence on the device: F[i*(M+1) + m] = F_m(T[i]), m = 0..M, T[i] >= 0.
  * Replaces computeBoysSequence (src/Integration/Engines/BoysFunction.jl:67-77) and
  * computeBoysFunc (:62-64).  path 0: the evaluator of the ERI class kernels (M <= 8);
@@ -185,6 +210,8 @@ typedef struct {
     int diis_size;          /* 1..15, default 15 (1 = no extrapolation) */
     double schwarz;         /* stored-integral screening Q_ab Q_cd >= schwarz, default 1e-14 */
     int iters_per_graph;    /* SCF iterations per CUDA-graph launch, default 4 */
+    const double* initial_density;  /* NULL: core-Hamiltonian guess; else per-spin densities
+                                       of all molecules, nfun x nfun each, concatenated */
 } qb_batch_config;
 
 typedef struct {
@@ -198,6 +225,7 @@ typedef struct {
     int64_t prim_quartets;  /* primitive quartets evaluated for them */
     int64_t eri_doubles;    /* stored integrals */
     int graph_launches;
+    double* density;        /* NULL or room for the final per-spin densities, concatenated */
 } qb_batch_result;
 
 void qb_batch_config_default(qb_batch_config* cfg);

@@ -21,7 +21,9 @@ EXPORTED = ["qb_create", "qb_destroy", "qb_last_error", "qb_device_info", "qb_ov
             "qb_nuc_attractions", "qb_core_hamiltonian", "qb_elec_repulsions", "qb_elec_repulsion_list", "qb_jk",
             "qb_jk_prepare", "qb_jk_upload_density", "qb_jk_execute", "qb_jk_download", "qb_jk_get_stats", "qb_jk_pair_table",
             "qb_scf_config_default", "qb_run_hartree_fock", "qb_fp64_peak", "qb_jk_noalloc", "qb_boys", "qb_multipole_moments",
-            "qb_batch_config_default", "qb_run_rhf_batched", "qb_jk_autotune"]
+            "qb_batch_config_default", "qb_run_rhf_batched", "qb_jk_autotune",
+            "qb_bf16_gemm_nt", "qb_gelu_forward", "qb_gelu_backward", "qb_f32_to_bf16", "qb_bf16_transpose",
+            "qb_colsum", "qb_mse_grad", "qb_adam_step"]
 
 
 class DimensionMismatch(ValueError):
@@ -163,14 +165,16 @@ class Context:
 
 class QBBatchConfig(C.Structure):
     _fields_ = [("conv_energy", C.c_double), ("conv_density", C.c_double), ("max_iter", C.c_int),
-                ("diis_size", C.c_int), ("schwarz", C.c_double), ("iters_per_graph", C.c_int)]
+                ("diis_size", C.c_int), ("schwarz", C.c_double), ("iters_per_graph", C.c_int),
+                ("initial_density", C.POINTER(C.c_double))]
 
 
 class QBBatchResult(C.Structure):
     _fields_ = [("energy", C.POINTER(C.c_double)), ("iterations", C.POINTER(C.c_int)),
                 ("converged", C.POINTER(C.c_int)), ("jacobi_sweeps", C.POINTER(C.c_int)),
                 ("ms_integrals", C.c_double), ("ms_scf", C.c_double), ("quartets", C.c_int64),
-                ("prim_quartets", C.c_int64), ("eri_doubles", C.c_int64), ("graph_launches", C.c_int)]
+                ("prim_quartets", C.c_int64), ("eri_doubles", C.c_int64), ("graph_launches", C.c_int),
+                ("density", C.POINTER(C.c_double))]
 
 
 class BasisArgs:

@@ -358,9 +358,11 @@ class BatchSCFResult:
     prim_quartets: int
     eri_doubles: int
     graph_launches: int
+    densities: Optional[list] = None   # final per-spin densities (return_densities=True)
 
 
-def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ctx=None) -> BatchSCFResult:
+def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ctx=None,
+                          initial_densities=None, return_densities=False) -> BatchSCFResult:
     """Closed-shell HF of many molecules in one call (qb_run_rhf_batched).
 
     molecules: sequence of (nucInfo, basis) or (nucInfo, basis, charge); nucInfo a
@@ -391,18 +393,37 @@ def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ct
     Z = np.ascontiguousarray(np.concatenate(Zs), np.float64)
     R = np.ascontiguousarray(np.concatenate(Rs), np.float64)
     nocc_a = np.ascontiguousarray(nocc, np.int32)
+    d0 = None
+    if initial_densities is not None:
+        if len(initial_densities) != nmol:
+            raise DimensionMismatch("one initial density per molecule")
+        parts = []
+        for D, n in zip(initial_densities, nf):
+            D = np.asarray(D, dtype=np.float64)
+            if D.shape != (n, n):
+                raise DimensionMismatch("initial density shape")
+            parts.append(D.reshape(-1, order="F"))
+        d0 = np.ascontiguousarray(np.concatenate(parts))
     qcfg = L.QBBatchConfig(cfg.conv_energy, cfg.conv_density, cfg.max_iter, cfg.diis_size, cfg.schwarz,
-                           cfg.iters_per_graph)
+                           cfg.iters_per_graph, L.dptr(d0) if d0 is not None else None)
     E = np.zeros(nmol)
     it = np.zeros(nmol, np.int32)
     conv = np.zeros(nmol, np.int32)
     sw = np.zeros(nmol, np.int32)
-    res = L.QBBatchResult(L.dptr(E), L.iptr(it), L.iptr(conv), L.iptr(sw), 0.0, 0.0, 0, 0, 0, 0)
+    dout = np.zeros(sum(n * n for n in nf)) if return_densities else None
+    res = L.QBBatchResult(L.dptr(E), L.iptr(it), L.iptr(conv), L.iptr(sw), 0.0, 0.0, 0, 0, 0, 0,
+                          L.dptr(dout) if dout is not None else None)
     c.check(c.lib.qb_run_rhf_batched(c.h, nmol, bases, L.iptr(nnuc_a), L.dptr(Z), L.dptr(R), L.iptr(nocc_a),
                                      C.byref(qcfg), C.byref(res)))
+    dens = None
+    if dout is not None:
+        dens, off = [], 0
+        for n in nf:
+            dens.append(dout[off:off + n * n].reshape((n, n), order="F"))
+            off += n * n
     return BatchSCFResult(E + np.array(enn), E, it, conv.astype(bool), sw, np.array(nf), res.ms_integrals,
                           res.ms_scf, int(res.quartets), int(res.prim_quartets), int(res.eri_doubles),
-                          int(res.graph_launches))
+                          int(res.graph_launches), dens)
 
 
 def fp64_peak(ctx=None):

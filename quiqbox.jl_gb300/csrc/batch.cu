@@ -121,8 +121,10 @@ __global__ void __launch_bounds__(128) qb_batch_digest_kernel(const BatchWork w,
     }
 }
 
-// X = S^{-1/2} by the eigen-decomposition of S; C' = I, D = D' = 0.
-__global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_orth_kernel(MolDev* mols, int* failed) {
+// X = S^{-1/2} by the eigen-decomposition of S; C' = I; D = D' = 0, or with an initial
+// density D0 (already in D): D' = S^{1/2} D0 S^{1/2}, D~ = ratio-scaled D0, and the SCF
+// starts at iteration 1 (the first step builds F from D0).
+__global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_orth_kernel(MolDev* mols, int* failed, int have_d0) {
     __shared__ QbJacobiSmem<QB_BATCH_MAXN> jsm;
     MolDev& M = mols[blockIdx.x];
     const int n = M.n, nn = n * n, tid = threadIdx.x, nt = blockDim.x;
@@ -146,11 +148,25 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_orth_kernel(MolDev*
     qb_cta_gemm(false, true, n, n, n, 1.0, M.W2, n, M.W1, n, 0.0, M.X, n);
     for (int i = tid; i < nn; i += nt) {
         M.Cp[i] = ((i % n) == (i / n)) ? 1.0 : 0.0;
-        M.D[i] = 0.0;
-        M.Dt[i] = 0.0;
-        M.Do[i] = 0.0;
         M.Jp[i] = 0.0;
         M.Kp[i] = 0.0;
+        if (!have_d0) {
+            M.D[i] = 0.0;
+            M.Dt[i] = 0.0;
+            M.Do[i] = 0.0;
+        }
+    }
+    __syncthreads();
+    if (have_d0) {
+        // S^{1/2} = S X (W1), D' = W1 D0 W1^T
+        qb_cta_gemm(false, false, n, n, n, 1.0, M.S, n, M.X, n, 0.0, M.W1, n);
+        qb_cta_gemm(false, false, n, n, n, 1.0, M.W1, n, M.D, n, 0.0, M.W2, n);
+        qb_cta_gemm(false, true, n, n, n, 1.0, M.W2, n, M.W1, n, 0.0, M.Do, n);
+        for (int idx = tid; idx < nn; idx += nt) {
+            const int i = idx % n, j = idx / n;
+            M.Dt[idx] = M.D[idx] * M.ratio[i] * M.ratio[j];
+        }
+        if (tid == 0) M.iter = 1;
     }
 }
 
@@ -393,6 +409,7 @@ extern "C" void qb_batch_config_default(qb_batch_config* cfg) {
     cfg->diis_size = QB_BATCH_DIIS;
     cfg->schwarz = 1e-14;
     cfg->iters_per_graph = 4;
+    cfg->initial_density = nullptr;
 }
 
 int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nnuc, const double* Z,
@@ -692,7 +709,10 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     DevArray<int> d_counters;   // [0] failed, [1] active
     QB_CUDA(ctx, d_counters.ensure(2));
     QB_CUDA(ctx, cudaMemsetAsync(d_counters.p, 0, 2 * sizeof(int), s));
-    qb_batch_orth_kernel<<<nmol, QB_BATCH_THREADS, 0, s>>>(d_mols.p, d_counters.p);
+    if (cfg.initial_density)
+        QB_CUDA(ctx, cudaMemcpyAsync(d_mats.p + 4 * (size_t)NN, cfg.initial_density, NN * sizeof(double),
+                                     cudaMemcpyHostToDevice, s));
+    qb_batch_orth_kernel<<<nmol, QB_BATCH_THREADS, 0, s>>>(d_mols.p, d_counters.p, cfg.initial_density ? 1 : 0);
     QB_CUDA(ctx, cudaGetLastError());
     QB_CUDA(ctx, cudaEventRecord(ev1, s));
     QB_TRY(qb_check_status(ctx));
@@ -737,6 +757,8 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     QB_TRY(rc);
     QB_CUDA(ctx, cudaEventRecord(ev2, s));
     QB_CUDA(ctx, cudaMemcpyAsync(hm.data(), d_mols.p, nmol * sizeof(MolDev), cudaMemcpyDeviceToHost, s));
+    if (res->density)
+        QB_CUDA(ctx, cudaMemcpyAsync(res->density, d_mats.p + 4 * (size_t)NN, NN * sizeof(double), cudaMemcpyDeviceToHost, s));
     unsigned long long nprimq = 0;
     QB_CUDA(ctx, cudaMemcpyAsync(&nprimq, d_primcount.p, sizeof(nprimq), cudaMemcpyDeviceToHost, s));
     QB_CUDA(ctx, cudaStreamSynchronize(s));

@@ -1,0 +1,91 @@
+"""Learned initial guess on the GPU: the BF16 tensor-core GEMM, the MLP's forward and
+backward kernels against the CPU oracle (oracle/mlp_oracle.py, same BF16 rounding
+points), training, and what the trained network gains over the core-Hamiltonian guess."""
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+sys.path.insert(0, str(Path(__file__).resolve().parents[1] / "oracle"))
+
+
+def _lib(qb):
+    from quiqbox_gb300 import _lib as L
+    return L.load()
+
+
+def test_bf16_gemm_vs_numpy(qb):
+    torch = pytest.importorskip("torch")
+    import mlp_oracle as mo
+    from quiqbox_gb300.guess import GuessMLP
+    net = GuessMLP(_lib(qb))
+    rng = np.random.default_rng(0)
+    for M, N, K in ((64, 64, 32), (128, 256, 64), (4096, 64, 256), (256, 128, 4096)):
+        A = mo.bf16(rng.normal(size=(M, K)))
+        B = mo.bf16(rng.normal(size=(N, K)))
+        bias = rng.normal(size=N).astype(np.float32)
+        Ad = net.to_bf16(torch.tensor(A, dtype=torch.float32, device="cuda"))
+        Bd = net.to_bf16(torch.tensor(B, dtype=torch.float32, device="cuda"))
+        Cd = net.gemm(Ad, Bd, torch.tensor(bias, device="cuda"), M, N, K).cpu().numpy()
+        ref = A @ B.T + bias
+        assert np.abs(Cd - ref).max() <= 1e-5 * np.abs(ref).max() + 1e-5, (M, N, K)
+
+
+def test_mlp_forward_backward_vs_oracle(qb):
+    torch = pytest.importorskip("torch")
+    import mlp_oracle as mo
+    from quiqbox_gb300.guess import GuessMLP
+    net = GuessMLP(_lib(qb), seed=3)
+    rng = np.random.default_rng(4)
+    X = rng.normal(size=(128, 64)).astype(np.float32)
+    T = rng.normal(size=(128, 64)).astype(np.float32)
+    Wt = (rng.uniform(size=(128, 64)) < 0.4).astype(np.float32)
+    params = net.params()
+    xb = net.to_bf16(torch.tensor(X, device="cuda"))
+    Y, saved = net.forward(xb)
+    loss, dY = net.loss_grad(Y, torch.tensor(T, device="cuda"), torch.tensor(Wt, device="cuda"))
+    dW, db = net.backward(dY, saved)
+    Yr, sr = mo.forward(params, X, round=True)
+    lr, dYr = mo.mse(Yr, T, Wt)
+    assert np.abs(Y.cpu().numpy() - Yr).max() <= 2e-3 * np.abs(Yr).max()
+    assert float(loss.item()) == pytest.approx(lr, rel=1e-3)
+    dWr, dbr = mo.backward(params, sr, dY.cpu().numpy().astype(np.float64), round=True)
+    for l in range(len(dWr)):
+        g, gr = dW[l].cpu().numpy(), dWr[l]
+        assert np.abs(g - gr).max() <= 2e-2 * np.abs(gr).max(), l
+        assert np.abs(db[l].cpu().numpy() - dbr[l]).max() <= 2e-2 * np.abs(dbr[l]).max() + 1e-7, l
+
+
+def test_training_reduces_loss_on_scf_labels(qb):
+    pytest.importorskip("torch")
+    from quiqbox_gb300 import guess
+    from quiqbox_gb300.workloads import batch_molecules
+    mols = batch_molecules(96, seed=11, atoms=(3, 8), basis_names=("STO-3G",))
+    res = qb.runHartreeFockBatched([(m["nuc"], m["flat"], m["charge"]) for m in mols], return_densities=True)
+    keep = [k for k in range(len(mols)) if res.converged[k]]
+    X, Y, W = guess.dataset([mols[k] for k in keep], [res.densities[k] for k in keep])
+    net = guess.GuessMLP(_lib(qb), seed=1)
+    hist = guess.train(net, X, Y, W, epochs=40, batch=256, lr=2e-3)
+    assert hist[-1] < 0.2 * hist[0]
+
+
+def test_learned_guess_gains_over_coreh(qb):
+    # the committed network on held-out molecules (not in its training set): the SCF from
+    # the learned density converges to the same energies in fewer iterations
+    pytest.importorskip("torch")
+    from quiqbox_gb300 import guess
+    from quiqbox_gb300.workloads import batch_molecules
+    if not guess.WEIGHTS_FILE.exists():
+        pytest.skip("no trained weights")
+    net = guess.load(_lib(qb))
+    mols = batch_molecules(200, seed=303, atoms=(3, 12), basis_names=("STO-3G",))
+    args = [(m["nuc"], m["flat"], m["charge"]) for m in mols]
+    base = qb.runHartreeFockBatched(args)
+    lrn, redo = guess.solve_with_guess(qb, net, mols)
+    both = base.converged & lrn.converged
+    assert both.mean() > 0.85
+    dE = np.abs(base.energies[both] - lrn.energies[both])
+    assert (dE < 1e-8).mean() > 0.9          # same SCF state for nearly all
+    assert lrn.iterations[both].mean() < 0.8 * base.iterations[both].mean()
