@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--batch-mols", type=int, default=512,
                     help="molecules of the batched-RHF measurement (0 skips it)")
     ap.add_argument("--batch-cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--guess-mols", type=int, default=2000,
+                    help="held-out molecules of the learned-guess measurement (0 skips it)")
     ap.add_argument("--jk-only", type=int, default=0,
                     help="profiling driver: prepare the workload, run this many J/K builds, print timings, exit")
     return ap.parse_args()
@@ -395,6 +397,8 @@ def run_ours(args):
         line["cpu_baseline"].pop("quartets", None)
         if args.batch_mols > 0:
             line["batched_rhf"] = batched_rhf(qb, args.batch_mols, args.seed, args.batch_cpu_seconds)
+        if args.guess_mols > 0:
+            line["learned_guess"] = learned_guess(qb, args.guess_mols)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -452,6 +456,19 @@ def batched_rhf(qb, n_mol, seed, cpu_seconds):
                                      f"{t_cpu:.1f} s of CPU work"}
     out["max_abs_dE_vs_oracle_on_sample"] = float(max(diffs)) if diffs else None
     return out
+
+
+def learned_guess(qb, n_mol):
+    """Config-4 measurement: held-out molecules (3-12 atoms, STO-3G) solved by the batched
+    SCF from the core-Hamiltonian guess and from the committed network's guess (with the
+    core-Hamiltonian fallback for the ones it does not converge)."""
+    from quiqbox_gb300 import guess, _lib as L
+    net = guess.load(L.load())
+    ev = guess.evaluate(qb, net, n_mol, seed=202)
+    ev["workload"] = ("held-out seeded chains of 3-12 atoms (H:C:N:O = 5:3:1:1), STO-3G, neutral or +1; "
+                      "batched RHF, DIIS, |dE| <= 1e-10, RMS(dD) <= 1e-8; network: 4 x 256 GELU MLP, "
+                      "BF16 weights, FP32 accumulation, trained on 19 038 molecules")
+    return ev
 
 
 def run_jk_only(args):

@@ -80,9 +80,11 @@ __device__ int qb_cta_jacobi(int n, double* A, double* V, const double* Vin, dou
             tot += a * a;
             if ((i % n) != (i / n)) off += a * a;
         }
-        off = qb_cta_sum(off, sm.red);
+        off = qb_cta_sum(off, sm.red);   // block-uniform
         tot = qb_cta_sum(tot, sm.red);
-        if (off <= 1e-30 * tot || off == 0.0 || (sweep > 0 && sm.rotated == 0) ||
+        const int rotated = sm.rotated;   // every thread reads the flag before it is reset
+        __syncthreads();
+        if (off <= 1e-30 * tot || off == 0.0 || (sweep > 0 && rotated == 0) ||
             (sweep > 0 && off <= 1e-24 * tot && off > 0.25 * off_prev)) {
             used = sweep;
             break;

@@ -8,17 +8,14 @@ whose guesses are CoreH / GWH / SAD / Direct (src/HartreeFock.jl:162-293); the s
 plugs into is the initial-density input of the batched SCF, the analogue of
 OrbCoeffInitialConfig(:Direct) (HartreeFock.jl:162-172).
 
-Network: 64 inputs -> 4 hidden layers of width 256 with GELU -> 64 outputs (25 used: a
+Network: 128 inputs -> 4 hidden layers of width 256 with GELU -> 64 outputs (25 used: a
 5 x 5 block), BF16 weights and activations, FP32 accumulation and FP32 master weights
 for Adam.  Every GPU operation is a kernel of this library (csrc/mlp.cu) called through
 the C ABI; torch only provides device memory and the stream.
 
-Features of the pair (A, B) (49 used, padded to 64): 32 Gaussian-expanded distances
-exp(-((r_AB - mu_k) / 0.25)^2), mu_k = 0.25 .. 8 bohr; a same-atom flag; element
-one-hots of A and B; per endpoint a smooth count of neighbouring H/C/N/O atoms
-(sum exp(-(r / 2.5)^2)).  Blocks live in a local frame whose z axis is A -> B, so the
-p components are predicted frame-independently and rotated back (D_lab = T_A D_loc T_B^T
-with T = diag(1, 1, R)).
+Features of the pair (A, B) are described at pair_data; blocks live in a local frame
+(z along A -> B, x towards a neighbouring atom), so the p components are predicted
+frame-independently and rotated back (D_lab = T_A D_loc T_B^T with T = diag(1, 1, R)).
 """
 from __future__ import annotations
 
@@ -32,34 +29,16 @@ import numpy as np
 
 ELEMENTS = ("H", "C", "N", "O")
 NBASIS = {"H": 1, "C": 5, "N": 5, "O": 5}
-NIN, NHID, NLAYER, NOUT = 64, 256, 4, 64
-NFEAT = 49
+NIN, NHID, NLAYER, NOUT = 128, 256, 4, 64
+NFEAT = 74
 MU = 0.25 + 0.25 * np.arange(32)
 WEIGHTS_FILE = Path(__file__).resolve().parent / "data" / "guess_mlp.npz"
 
 
 # ---------------------------------------------------------------------------
-# features and blocks
-def _frame(ra, rb):
-    """Rotation R (columns = local x, y, z axes in lab coordinates); z along A -> B."""
-    d = np.asarray(rb, float) - np.asarray(ra, float)
-    r = np.linalg.norm(d)
-    if r < 1e-12:
-        return np.eye(3)
-    z = d / r
-    ref = np.array([0.0, 0.0, 1.0]) if abs(z[2]) < 0.9 else np.array([1.0, 0.0, 0.0])
-    x = np.cross(ref, z)
-    x /= np.linalg.norm(x)
-    y = np.cross(z, x)
-    return np.stack([x, y, z], axis=1)
-
-
-def _T(sym, R):
-    n = NBASIS[sym]
-    T = np.eye(n)
-    if n == 5:
-        T[2:, 2:] = R
-    return T
+# features and blocks, vectorised over every atom pair of every molecule
+def pair_list(symbols):
+    return [(a, b) for a in range(len(symbols)) for b in range(a, len(symbols))]
 
 
 def atom_offsets(symbols):
@@ -70,70 +49,149 @@ def atom_offsets(symbols):
     return off, o
 
 
-def pair_list(symbols):
-    return [(a, b) for a in range(len(symbols)) for b in range(a, len(symbols))]
+def _unit(v):
+    return v / np.maximum(np.linalg.norm(v, axis=-1, keepdims=True), 1e-300)
 
 
-def features(symbols, coords):
-    """(npairs, 64) float32 features of pair_list(symbols)."""
-    P = np.asarray(coords, float)
-    nat = len(symbols)
-    oh = np.zeros((nat, 4))
-    for i, s in enumerate(symbols):
-        oh[i, ELEMENTS.index(s)] = 1.0
-    dist = np.linalg.norm(P[:, None, :] - P[None, :, :], axis=2)
-    env = np.zeros((nat, 4))
-    for i in range(nat):
-        w = np.exp(-(dist[i] / 2.5) ** 2)
-        w[i] = 0.0
-        env[i] = w @ oh
-    pairs = pair_list(symbols)
-    X = np.zeros((len(pairs), NIN), np.float32)
-    for k, (a, b) in enumerate(pairs):
-        r = dist[a, b]
-        X[k, :32] = np.exp(-((r - MU) / 0.25) ** 2)
-        X[k, 32] = 1.0 if a == b else 0.0
-        X[k, 33:37] = oh[a]
-        X[k, 37:41] = oh[b]
-        X[k, 41:45] = env[a]
-        X[k, 45:49] = env[b]
-    return X
+def pair_data(mols):
+    """Pairs (a <= b) of every molecule with their local frames and features.
+
+    Local frame: for a != b, z along A -> B and x towards the atom nearest the bond
+    midpoint (its component perpendicular to z); for a == b, z towards the nearest
+    neighbour and x towards the second nearest.  Without such an atom x is any unit
+    vector perpendicular to z.  Features (74 used of NIN): 32 Gaussian-expanded r_AB, a
+    same-atom flag, element one-hots of A and B, per endpoint and per element of the
+    neighbours sum w (1, cos_z, cos_x, (3 cos_z^2 - 1) / 2) with w = exp(-(r / 2.5)^2)
+    in the local frame, and the molecular charge."""
+    nat = max(len(m["symbols"]) for m in mols)
+    nm = len(mols)
+    pos = np.zeros((nm, nat, 3))
+    el = np.full((nm, nat), -1, np.int64)
+    for k, m in enumerate(mols):
+        na = len(m["symbols"])
+        pos[k, :na] = np.asarray(m["coords"], float)
+        el[k, :na] = [ELEMENTS.index(x) for x in m["symbols"]]
+    pm, pa, pb = [], [], []
+    for k, m in enumerate(mols):
+        na = len(m["symbols"])
+        ia, ib = np.triu_indices(na)
+        pm.append(np.full(len(ia), k))
+        pa.append(ia)
+        pb.append(ib)
+    pm, pa, pb = np.concatenate(pm), np.concatenate(pa), np.concatenate(pb)
+    npair = len(pm)
+    PA, PB = pos[pm, pa], pos[pm, pb]
+    same = pa == pb
+    neigh = pos[pm]                                   # (npair, nat, 3)
+    nel = el[pm]                                      # (npair, nat)
+    valid = nel >= 0
+    idx = np.arange(nat)[None, :]
+    dA = np.linalg.norm(neigh - PA[:, None, :], axis=2)
+    # z axis
+    z = _unit(PB - PA)
+    dA_other = np.where(valid & (idx != pa[:, None]), dA, np.inf)
+    order = np.argsort(dA_other, axis=1)
+    n1 = order[:, 0]
+    z_same = _unit(neigh[np.arange(npair), n1] - PA)
+    has1 = np.isfinite(dA_other[np.arange(npair), n1])
+    z = np.where(same[:, None], np.where(has1[:, None], z_same, np.array([0.0, 0.0, 1.0])), z)
+    # x axis: reference atom (midpoint-nearest third atom, or second-nearest neighbour)
+    mid = 0.5 * (PA + PB)
+    dmid = np.linalg.norm(neigh - mid[:, None, :], axis=2)
+    excl = (idx == pa[:, None]) | (idx == pb[:, None])
+    rel = neigh - PA[:, None, :]
+    perp = rel - np.sum(rel * z[:, None, :], axis=2, keepdims=True) * z[:, None, :]
+    pn = np.linalg.norm(perp, axis=2)
+    cand_pair = np.where(valid & ~excl & (pn > 0.3), dmid, np.inf)
+    cand_same = np.where(valid & (idx != pa[:, None]) & (idx != n1[:, None]) & (pn > 0.3), dA, np.inf)
+    cand = np.where(same[:, None], cand_same, cand_pair)
+    ref_i = np.argmin(cand, axis=1)
+    has_ref = np.isfinite(cand[np.arange(npair), ref_i])
+    xr = perp[np.arange(npair), ref_i]
+    helper = np.where(np.abs(z[:, 2:3]) < 0.9, np.array([0.0, 0.0, 1.0]), np.array([1.0, 0.0, 0.0]))
+    xa = np.cross(helper, z)
+    x = _unit(np.where(has_ref[:, None], xr, xa))
+    y = np.cross(z, x)
+    R = np.stack([x, y, z], axis=2)                  # columns: local axes in lab coordinates
+    # features
+    X = np.zeros((npair, NIN), np.float32)
+    r = np.linalg.norm(PB - PA, axis=1)
+    X[:, :32] = np.exp(-((r[:, None] - MU[None, :]) / 0.25) ** 2)
+    X[:, 32] = same
+    X[np.arange(npair), 33 + el[pm, pa]] = 1.0
+    X[np.arange(npair), 37 + el[pm, pb]] = 1.0
+    for e_off, (P, me) in enumerate(((PA, pa), (PB, pb))):
+        u = neigh - P[:, None, :]
+        d = np.linalg.norm(u, axis=2)
+        w = np.where(valid & (idx != me[:, None]), np.exp(-(d / 2.5) ** 2), 0.0)
+        dn = np.maximum(d, 1e-12)
+        cz = np.sum(u * z[:, None, :], axis=2) / dn
+        cx = np.sum(u * x[:, None, :], axis=2) / dn
+        terms = np.stack([w, w * cz, w * cx, w * 0.5 * (3 * cz * cz - 1)], axis=2)   # (npair, nat, 4)
+        for e in range(4):
+            sel = (nel == e)[:, :, None]
+            X[:, 41 + 16 * e_off + 4 * e:41 + 16 * e_off + 4 * e + 4] = np.sum(terms * sel, axis=1)
+    X[:, 73] = np.array([m["charge"] for m in mols], np.float32)[pm]
+    return {"mol": pm, "a": pa, "b": pb, "R": R, "X": X}
 
 
-def blocks_from_density(symbols, coords, D):
-    """Targets (npairs, 64) and weights (npairs, 64): local-frame blocks of D."""
-    off, _ = atom_offsets(symbols)
-    pairs = pair_list(symbols)
-    Y = np.zeros((len(pairs), NOUT), np.float32)
-    W = np.zeros((len(pairs), NOUT), np.float32)
-    for k, (a, b) in enumerate(pairs):
-        R = _frame(coords[a], coords[b])
-        na, nb = NBASIS[symbols[a]], NBASIS[symbols[b]]
-        blk = D[off[a]:off[a] + na, off[b]:off[b] + nb]
-        loc = _T(symbols[a], R).T @ blk @ _T(symbols[b], R)
-        full = np.zeros((5, 5))
-        full[:na, :nb] = loc
-        msk = np.zeros((5, 5))
-        msk[:na, :nb] = 1.0
-        Y[k, :25] = full.reshape(-1)
-        W[k, :25] = msk.reshape(-1)
-    return Y, W
-
-
-def density_from_blocks(symbols, coords, Ypred):
-    """Symmetric density assembled from predicted local-frame blocks."""
+def _gather_index(symbols):
+    """Per atom the 5 function indices of its padded block (n = dummy row/column)."""
     off, n = atom_offsets(symbols)
-    D = np.zeros((n, n))
-    for k, (a, b) in enumerate(pair_list(symbols)):
-        R = _frame(coords[a], coords[b])
-        na, nb = NBASIS[symbols[a]], NBASIS[symbols[b]]
-        loc = np.asarray(Ypred[k, :25], float).reshape(5, 5)[:na, :nb]
-        blk = _T(symbols[a], R) @ loc @ _T(symbols[b], R).T
-        if a == b:
-            blk = 0.5 * (blk + blk.T)
-        D[off[a]:off[a] + na, off[b]:off[b] + nb] = blk
-        D[off[b]:off[b] + nb, off[a]:off[a] + na] = blk.T
-    return D
+    out = np.full((len(symbols), 5), n, np.int64)
+    for i, sy in enumerate(symbols):
+        out[i, :NBASIS[sy]] = off[i] + np.arange(NBASIS[sy])
+    return out, n
+
+
+def _T5(R):
+    T = np.zeros((R.shape[0], 5, 5))
+    T[:, 0, 0] = T[:, 1, 1] = 1.0
+    T[:, 2:, 2:] = R
+    return T
+
+
+def blocks_from_densities(mols, dens, pd):
+    """Local-frame blocks (targets) and their masks, (npair, 64) each."""
+    Y = np.zeros((len(pd["mol"]), NOUT), np.float32)
+    Wm = np.zeros_like(Y)
+    T = _T5(pd["R"])
+    start = 0
+    for k, (m, D) in enumerate(zip(mols, dens)):
+        gi, n = _gather_index(m["symbols"])
+        cnt = len(m["symbols"]) * (len(m["symbols"]) + 1) // 2
+        sl = slice(start, start + cnt)
+        Dp = np.zeros((n + 1, n + 1))
+        Dp[:n, :n] = D
+        ia, ib = gi[pd["a"][sl]], gi[pd["b"][sl]]
+        blk = Dp[ia[:, :, None], ib[:, None, :]]
+        loc = np.einsum("pji,pjk,pkl->pil", T[sl], blk, T[sl])
+        mask = ((ia < n)[:, :, None] & (ib < n)[:, None, :]).astype(np.float32)
+        Y[sl, :25] = (loc * mask).reshape(cnt, 25)
+        Wm[sl, :25] = mask.reshape(cnt, 25)
+        start += cnt
+    return Y, Wm
+
+
+def densities_from_blocks(mols, pd, Ypred):
+    T = _T5(pd["R"])
+    out, start = [], 0
+    for m in mols:
+        gi, n = _gather_index(m["symbols"])
+        cnt = len(m["symbols"]) * (len(m["symbols"]) + 1) // 2
+        sl = slice(start, start + cnt)
+        loc = np.asarray(Ypred[sl, :25], float).reshape(cnt, 5, 5)
+        blk = np.einsum("pij,pjk,plk->pil", T[sl], loc, T[sl])
+        a, b = pd["a"][sl], pd["b"][sl]
+        diag = a == b
+        blk[diag] = 0.5 * (blk[diag] + np.transpose(blk[diag], (0, 2, 1)))
+        Dp = np.zeros((n + 1, n + 1))
+        ia, ib = gi[a], gi[b]
+        Dp[ib[:, :, None], ia[:, None, :]] = np.transpose(blk, (0, 2, 1))
+        Dp[ia[:, :, None], ib[:, None, :]] = blk
+        out.append(Dp[:n, :n].copy())
+        start += cnt
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -292,13 +350,9 @@ def _pad_rows(a, mult=64):
 
 # ---------------------------------------------------------------------------
 def dataset(mols, densities):
-    X, Y, W = [], [], []
-    for m, D in zip(mols, densities):
-        X.append(features(m["symbols"], m["coords"]))
-        y, w = blocks_from_density(m["symbols"], m["coords"], D)
-        Y.append(y)
-        W.append(w)
-    return np.concatenate(X), np.concatenate(Y), np.concatenate(W)
+    pd = pair_data(mols)
+    Y, W = blocks_from_densities(mols, densities, pd)
+    return pd["X"], Y, W
 
 
 def train(net, X, Y, W, epochs=20, batch=4096, lr=1e-3, seed=0, log=None):
@@ -336,14 +390,8 @@ def load(lib, device="cuda:0", path=WEIGHTS_FILE):
 
 def initial_densities(net, mols):
     """Learned initial per-spin densities of a list of generated molecules."""
-    X = [features(m["symbols"], m["coords"]) for m in mols]
-    counts = [x.shape[0] for x in X]
-    Yp = net.predict(np.concatenate(X))
-    out, o = [], 0
-    for m, c in zip(mols, counts):
-        out.append(density_from_blocks(m["symbols"], m["coords"], Yp[o:o + c]))
-        o += c
-    return out
+    pd = pair_data(mols)
+    return densities_from_blocks(mols, pd, net.predict(pd["X"]))
 
 
 def train_main(n_train=20000, n_test=2000, seed_train=101, seed_test=202, epochs=20, out=WEIGHTS_FILE,

@@ -61,20 +61,41 @@ def test_guess_blocks_round_trip():
     ge.load_package()
     from quiqbox_gb300 import guess
     from quiqbox_gb300.workloads import batch_molecules
-    for m in batch_molecules(5, seed=9, atoms=(3, 8), basis_names=("STO-3G",)):
+    mols = batch_molecules(12, seed=9, atoms=(2, 10), basis_names=("STO-3G",))
+    pd = guess.pair_data(mols)
+    rng = np.random.default_rng(1)
+    dens = []
+    for m in mols:
         _, n = guess.atom_offsets(m["symbols"])
         assert n == m["flat"].nfun
-        rng = np.random.default_rng(1)
         A = rng.normal(size=(n, n))
-        D = A + A.T
-        Y, W = guess.blocks_from_density(m["symbols"], m["coords"], D)
-        D2 = guess.density_from_blocks(m["symbols"], m["coords"], Y)
-        assert np.abs(D2 - D).max() < 1e-6
-        X = guess.features(m["symbols"], m["coords"])
-        assert X.shape == (len(guess.pair_list(m["symbols"])), 64) and np.isfinite(X).all()
-        # rotating the molecule leaves features and local-frame blocks unchanged for a ≠ b
-        R = np.linalg.qr(rng.normal(size=(3, 3)))[0]
-        if np.linalg.det(R) < 0:
-            R[:, 0] *= -1
-        c2 = [tuple(R @ np.array(c)) for c in m["coords"]]
-        assert np.abs(guess.features(m["symbols"], c2) - X).max() < 1e-5
+        dens.append(A + A.T)
+    Y, W = guess.blocks_from_densities(mols, dens, pd)
+    D2 = guess.densities_from_blocks(mols, pd, Y)
+    assert max(np.abs(a - b).max() for a, b in zip(dens, D2)) < 1e-5
+    R = pd["R"]
+    assert np.abs(np.einsum("pij,pik->pjk", R, R) - np.eye(3)).max() < 1e-12
+    assert np.abs(np.linalg.det(R) - 1.0).max() < 1e-12
+    assert pd["X"].shape == (len(pd["mol"]), guess.NIN) and np.isfinite(pd["X"]).all()
+    # rotating and translating every molecule leaves the features and the local-frame
+    # blocks of the rotated densities unchanged
+    Q = np.linalg.qr(rng.normal(size=(3, 3)))[0]
+    if np.linalg.det(Q) < 0:
+        Q[:, 0] *= -1
+    rot = []
+    for m in mols:
+        m2 = dict(m)
+        m2["coords"] = [tuple(Q @ np.array(c) + 1.5) for c in m["coords"]]
+        rot.append(m2)
+    pd2 = guess.pair_data(rot)
+    assert np.abs(pd2["X"] - pd["X"]).max() < 1e-5
+    dens2 = []
+    for m, D in zip(mols, dens):
+        T = np.eye(len(D))
+        off, _ = guess.atom_offsets(m["symbols"])
+        for i, s in enumerate(m["symbols"]):
+            if guess.NBASIS[s] == 5:
+                T[off[i] + 2:off[i] + 5, off[i] + 2:off[i] + 5] = Q
+        dens2.append(T @ D @ T.T)
+    Y2, _ = guess.blocks_from_densities(rot, dens2, pd2)
+    assert np.abs(Y2 - Y).max() < 1e-5
