@@ -63,22 +63,21 @@ def pair_data(mols):
     same-atom flag, element one-hots of A and B, per endpoint and per element of the
     neighbours sum w (1, cos_z, cos_x, (3 cos_z^2 - 1) / 2) with w = exp(-(r / 2.5)^2)
     in the local frame, and the molecular charge."""
-    nat = max(len(m["symbols"]) for m in mols)
+    nats = np.array([len(m["symbols"]) for m in mols])
+    nat = int(nats.max())
     nm = len(mols)
     pos = np.zeros((nm, nat, 3))
     el = np.full((nm, nat), -1, np.int64)
+    code = {e: i for i, e in enumerate(ELEMENTS)}
     for k, m in enumerate(mols):
-        na = len(m["symbols"])
-        pos[k, :na] = np.asarray(m["coords"], float)
-        el[k, :na] = [ELEMENTS.index(x) for x in m["symbols"]]
-    pm, pa, pb = [], [], []
-    for k, m in enumerate(mols):
-        na = len(m["symbols"])
-        ia, ib = np.triu_indices(na)
-        pm.append(np.full(len(ia), k))
-        pa.append(ia)
-        pb.append(ib)
-    pm, pa, pb = np.concatenate(pm), np.concatenate(pa), np.concatenate(pb)
+        na = nats[k]
+        pos[k, :na] = m["coords"]
+        el[k, :na] = [code[x] for x in m["symbols"]]
+    tri = {n: np.triu_indices(n) for n in np.unique(nats)}
+    cnt = nats * (nats + 1) // 2
+    pm = np.repeat(np.arange(nm), cnt)
+    pa = np.concatenate([tri[n][0] for n in nats])
+    pb = np.concatenate([tri[n][1] for n in nats])
     npair = len(pm)
     PA, PB = pos[pm, pa], pos[pm, pb]
     same = pa == pb
@@ -432,12 +431,14 @@ def train_main(n_train=20000, n_test=2000, seed_train=101, seed_test=202, epochs
     return info
 
 
-def solve_with_guess(qb, net, mols, fallback=True):
-    """Batched SCF from the learned guess; molecules it does not converge are solved again
-    from the core-Hamiltonian guess (the fallback).  Returns (result, fallback indices)."""
+def solve_with_guess(qb, net, mols, fallback=True, first_max_iter=100):
+    """Batched SCF from the learned guess; molecules it has not converged after
+    `first_max_iter` iterations are solved again from the core-Hamiltonian guess (the
+    fallback).  Returns (result, fallback indices)."""
     args = [(m["nuc"], m["flat"], m["charge"]) for m in mols]
     D0 = initial_densities(net, mols)
-    res = qb.runHartreeFockBatched(args, initial_densities=D0)
+    cfg = qb.BatchSCFConfig(max_iter=first_max_iter if fallback else 200)
+    res = qb.runHartreeFockBatched(args, config=cfg, initial_densities=D0)
     redo = [k for k in range(len(mols)) if not res.converged[k]] if fallback else []
     if redo:
         r2 = qb.runHartreeFockBatched([args[k] for k in redo])
