@@ -107,6 +107,15 @@ int qb_mse_grad(int64_t n, const float* y, const float* t, const float* w, float
 int qb_adam_step(int64_t n, float* w, const float* g, float* m, float* v, void* w_bf16, float lr, float b1, float b2,
                  float eps, int step, void* stream);
 
+/* Backward pass of the two-electron energy for basis-parameter gradients (the reference
+ * has no analytic gradient; src/Differentiation/Finite.jl holds finite-difference
+ * weights only).  Functions [0, n) of `basis` are the basis, [n, nfun) extra single
+ * primitives g (derivative primitives); P is the n x n total density.  Recomputes every
+ * (g nu|lambda sigma) (no storage) and returns, row-major ng x n,
+ *   Jx[g][nu] = sum (g nu|lambda sigma) P_{lambda sigma},
+ *   Kx[g][lambda] = sum (g nu|lambda sigma) P_{nu sigma}. */
+int qb_adjoint_jk(qb_ctx* ctx, const qb_basis* basis, int n, const double* P, double* Jx, double* Kx);
+
 /* Boys function sequence on the device: F[i*(M+1) + m] = F_m(T[i]), m = 0..M, T[i] >= 0.
  * Replaces computeBoysSequence (src/Integration/Engines/BoysFunction.jl:67-77) and
  * computeBoysFunc (:62-64).  path 0: the evaluator of the ERI class kernels (M <= 8);

@@ -16,3 +16,4 @@ from .api import (overlaps, overlap, elecKinetics, elecKinetic, nucAttractions, 
                   runHartreeFockBatched, BatchSCFConfig, BatchSCFResult, jk_autotune,
                   DimensionMismatch, DomainError)
 from ._lib import Context, load as load_library, LIB_PATH, EXPORTED  # noqa: F401
+from .differentiation import GaussShell, rhf_energy_gradient, rhf_energy  # noqa: F401

@@ -23,7 +23,7 @@ EXPORTED = ["qb_create", "qb_destroy", "qb_last_error", "qb_device_info", "qb_ov
             "qb_scf_config_default", "qb_run_hartree_fock", "qb_fp64_peak", "qb_jk_noalloc", "qb_boys", "qb_multipole_moments",
             "qb_batch_config_default", "qb_run_rhf_batched", "qb_jk_autotune",
             "qb_bf16_gemm_nt", "qb_gelu_forward", "qb_gelu_backward", "qb_f32_to_bf16", "qb_bf16_transpose",
-            "qb_colsum", "qb_mse_grad", "qb_adam_step"]
+            "qb_colsum", "qb_mse_grad", "qb_adam_step", "qb_adjoint_jk"]
 
 
 class DimensionMismatch(ValueError):

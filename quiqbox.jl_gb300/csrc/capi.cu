@@ -167,6 +167,26 @@ int qb_multipole_moments(qb_ctx* ctx, const qb_basis* basis, const double* cente
     return qb_check_status(ctx);
 }
 
+int qb_adjoint_jk(qb_ctx* ctx, const qb_basis* basis, int n, const double* P, double* Jx, double* Kx) {
+    QB_TRY(enter(ctx));
+    if (!basis || !P || !Jx || !Kx) return qb_set_error(ctx, QB_ERR_ARG, "null argument");
+    if (n < 1 || n >= basis->nfun) return qb_set_error(ctx, QB_ERR_DIM, "need 1 <= n < nfun (extra functions after n)");
+    QB_TRY(qb_set_basis(ctx, basis));
+    const int ng = ctx->nfun - n;
+    const size_t nn = (size_t)n * n, gn = (size_t)ng * n;
+    QB_CUDA(ctx, ctx->d_m0.ensure(nn));
+    QB_CUDA(ctx, ctx->d_m1.ensure(2 * gn));
+    QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_m0.p, P, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    QB_CUDA(ctx, cudaMemsetAsync(ctx->d_m1.p, 0, 2 * gn * sizeof(double), ctx->stream));
+    if (qb_gen_adjoint_eri(qb_gen_basis(ctx), n, ng, ctx->d_m0.p, ctx->boys.p, ctx->d_m1.p, ctx->d_m1.p + gn,
+                           ctx->status.p, ctx->nsm, ctx->stream) != 0)
+        return qb_cuda_check(ctx, cudaGetLastError(), "adjoint ERI kernel");
+    QB_CUDA(ctx, cudaMemcpyAsync(Jx, ctx->d_m1.p, gn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    QB_CUDA(ctx, cudaMemcpyAsync(Kx, ctx->d_m1.p + gn, gn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    QB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return qb_check_status(ctx);
+}
+
 int qb_elec_repulsions(qb_ctx* ctx, const qb_basis* basis, double* eri) {
     QB_TRY(enter(ctx));
     if (!eri) return qb_set_error(ctx, QB_ERR_ARG, "null output");

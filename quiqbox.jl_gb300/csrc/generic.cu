@@ -415,6 +415,45 @@ __global__ void qb_schwarz_generic_kernel(const GenBasis b, const double* __rest
     Q[k] = sqrt(mx);
 }
 
+// Adjoint (backward) pass of the two-electron energy: functions [n, n + ng) of the
+// basis are extra single primitives g (derivatives of the basis functions' primitives),
+// functions [0, n) the basis itself with the total density P (n x n).  For every g, every
+// nu and every canonical pair lambda >= sigma the integral (g nu | lambda sigma) is
+// recomputed (nothing stored) and digested into
+//   Jx[g][nu]     = sum_{lambda sigma} (g nu | lambda sigma) P_{lambda sigma}
+//   Kx[g][lambda] = sum_{nu sigma}     (g nu | lambda sigma) P_{nu sigma}.
+__global__ void qb_adjoint_eri_kernel(const GenBasis b, int n, int ng, const double* __restrict__ P,
+                                      const double* __restrict__ boys, double* Jx, double* Kx, int* status) {
+    const long long npair = (long long)n * (n + 1) / 2;
+    const long long total = (long long)ng * n * npair;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long pr = t % npair;
+        const long long rest = t / npair;
+        const int nu = (int)(rest % n), g = (int)(rest / n);
+        int lam, sig;
+        tri_decode(pr, lam, sig);
+        const double I = md_eri(b, n + g, nu, lam, sig, boys, status);
+        if (I == 0.0) continue;
+        const double w = (lam == sig) ? 1.0 : 2.0;
+        atomicAdd(Jx + (size_t)g * n + nu, w * I * P[lam + (size_t)n * sig]);
+        atomicAdd(Kx + (size_t)g * n + lam, I * P[nu + (size_t)n * sig]);
+        if (lam != sig) atomicAdd(Kx + (size_t)g * n + sig, I * P[nu + (size_t)n * lam]);
+    }
+}
+
+int qb_gen_adjoint_eri(const GenDevBasis& gb, int n, int ng, const double* P, const double* boys, double* Jx,
+                       double* Kx, int* status, int nsm, cudaStream_t s) {
+    GenBasis b{gb.fp, gb.cen, gb.ijk, gb.alpha, gb.w, gb.nfun};
+    const long long total = (long long)ng * n * ((long long)n * (n + 1) / 2);
+    const int block = 64;
+    long long grid = (total + block - 1) / block;
+    const long long cap = (long long)nsm * 32;
+    if (grid > cap) grid = cap;
+    if (grid > 0) qb_adjoint_eri_kernel<<<(unsigned)grid, block, 0, s>>>(b, n, ng, P, boys, Jx, Kx, status);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 // ---------------------------------------------------------------------------
 int qb_gen_onebody(const GenDevBasis& gb, int flags, int nnuc, const double* dZ, const double* dR,
                    const double* boys, double* S, double* T, double* V, int* status, cudaStream_t s) {

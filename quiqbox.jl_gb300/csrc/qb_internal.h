@@ -25,6 +25,8 @@ struct GenDevBasis {
 int qb_gen_onebody_batch(const GenDevBasis& gb, int nmol, long long npair_total, const long long* poff,
                          const int* fo, const int* nf, const long long* mo, const int* nuc0, const double* dZ,
                          const double* dR, const double* boys, double* S, double* H, int* status, cudaStream_t s);
+int qb_gen_adjoint_eri(const GenDevBasis& gb, int n, int ng, const double* P, const double* boys, double* Jx,
+                       double* Kx, int* status, int nsm, cudaStream_t s);
 int qb_gen_multipole(const GenDevBasis& gb, const double* C, const int* deg, double* M, int* status, cudaStream_t s);
 int qb_gen_onebody(const GenDevBasis& gb, int flags, int nnuc, const double* dZ, const double* dR,
                    const double* boys, double* S, double* T, double* V, int* status, cudaStream_t s);

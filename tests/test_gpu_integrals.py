@@ -1,6 +1,6 @@
 """One- and two-electron integrals on the GPU against the CPU oracle and the
 reference's golden values.  Tolerance: 1e-12 absolute on integrals (the
-spec parity bar), unless stated."""
+parity bar of the integral path), unless stated."""
 import numpy as np
 import pytest
 
