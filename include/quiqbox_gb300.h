@@ -116,6 +116,13 @@ int qb_adam_step(int64_t n, float* w, const float* g, float* m, float* v, void* 
  *   Kx[g][lambda] = sum (g nu|lambda sigma) P_{nu sigma}. */
 int qb_adjoint_jk(qb_ctx* ctx, const qb_basis* basis, int n, const double* P, double* Jx, double* Kx);
 
+/* k lowest eigenpairs of a symmetric n x n matrix A (column-major), n <= 1024: the
+ * batched SCF's eigensolver (Householder tridiagonalisation, bisection, inverse
+ * iteration).  w: k eigenvalues ascending; Y: n x k eigenvectors (column-major).  It
+ * replaces the eigen call of solveFockMatrix (src/HartreeFock.jl:46-56) where only the
+ * occupied orbitals are needed. */
+int qb_eigh_lowest(qb_ctx* ctx, int n, int k, const double* A, double* w, double* Y);
+
 /* Boys function sequence on the device: F[i*(M+1) + m] = F_m(T[i]), m = 0..M, T[i] >= 0.
  * Replaces computeBoysSequence (src/Integration/Engines/BoysFunction.jl:67-77) and
  * computeBoysFunc (:62-64).  path 0: the evaluator of the ERI class kernels (M <= 8);
@@ -221,6 +228,10 @@ typedef struct {
     int iters_per_graph;    /* SCF iterations per CUDA-graph launch, default 4 */
     const double* initial_density;  /* NULL: core-Hamiltonian guess; else per-spin densities
                                        of all molecules, nfun x nfun each, concatenated */
+    int eigensolver;        /* 0 (default): occupied eigenvectors by Householder tridiagonalisation,
+                               bisection and inverse iteration; 1: Jacobi over all eigenvectors */
+    int jacobi_sweeps;      /* eigensolver 1: sweeps per SCF iteration (eigenvectors carry over from
+                               the previous iteration); 0: until converged (default) */
 } qb_batch_config;
 
 typedef struct {

@@ -314,6 +314,18 @@ def jk_autotune(basis, D, schwarz=1e-12, repeats=1, ctx=None):
     return {"".join(str(v) for v in st.class_l[k]): int(chosen[k]) for k in range(st.nclass)}
 
 
+def eigh_lowest(A, k, ctx=None):
+    """k lowest eigenpairs of the symmetric matrix A on the device (qb_eigh_lowest)."""
+    c = _ctx(ctx)
+    A = np.asarray(A, dtype=np.float64)
+    n = A.shape[0]
+    Af = np.ascontiguousarray(A.reshape(-1, order="F"))
+    w = np.zeros(k)
+    Y = np.zeros(n * k)
+    c.check(c.lib.qb_eigh_lowest(c.h, n, k, L.dptr(Af), L.dptr(w), L.dptr(Y)))
+    return w, Y.reshape((n, k), order="F")
+
+
 def computeBoysSequence(T, M, path=0, ctx=None):
     """F_0..F_M at every T (array of shape T.shape + (M+1,)), evaluated on the device.
 
@@ -342,6 +354,8 @@ class BatchSCFConfig:
     diis_size: int = 15
     schwarz: float = 1e-14
     iters_per_graph: int = 4
+    eigensolver: int = 0          # 0: tridiagonal occupied-subspace solver; 1: Jacobi
+    jacobi_sweeps: int = 0        # Jacobi sweeps per SCF iteration; 0 = to convergence
 
 
 @dataclass
@@ -405,7 +419,8 @@ def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ct
             parts.append(D.reshape(-1, order="F"))
         d0 = np.ascontiguousarray(np.concatenate(parts))
     qcfg = L.QBBatchConfig(cfg.conv_energy, cfg.conv_density, cfg.max_iter, cfg.diis_size, cfg.schwarz,
-                           cfg.iters_per_graph, L.dptr(d0) if d0 is not None else None)
+                           cfg.iters_per_graph, L.dptr(d0) if d0 is not None else None, cfg.eigensolver,
+                           cfg.jacobi_sweeps)
     E = np.zeros(nmol)
     it = np.zeros(nmol, np.int32)
     conv = np.zeros(nmol, np.int32)

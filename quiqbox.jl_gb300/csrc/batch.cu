@@ -64,14 +64,14 @@ struct MolDev {
     int dlist[QB_BATCH_SLOTS];
     double dEs[QB_BATCH_SLOTS];   // per-spin energy of each slot's entry
     double E, Eprev, dE, rmsD;
-    double *S, *H, *X, *F, *D, *Dt, *Do, *Jp, *Kp, *Cp, *W1, *W2, *W3;
+    double *S, *H, *X, *F, *D, *Dt, *Do, *Jp, *Kp, *Cp, *W1, *W2, *W3, *W4, *W5, *W6;
     double *Fh, *Eh, *B, *eps, *wt;
     const double* ratio;
 };
 
 struct StepParams {
     double thr_e, thr_d;
-    int max_iter, diis;
+    int max_iter, diis, sweeps, eig;   // eig 0: tridiagonal occupied-subspace solver, 1: Jacobi
 };
 
 // ---------------------------------------------------------------------------
@@ -223,6 +223,7 @@ __device__ bool qb_diis_coeffs(int m, const double* B, const int* idx, double* c
 __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev* mols, const int* __restrict__ order,
                                                                          const StepParams prm, int* active) {
     __shared__ QbJacobiSmem<QB_BATCH_MAXN> jsm;
+    __shared__ QbEigSmem<QB_BATCH_MAXN> esm;
     __shared__ double red[33];
     __shared__ double s_c[QB_BATCH_SLOTS];
     __shared__ int s_idx[QB_BATCH_SLOTS], s_ok;
@@ -327,16 +328,30 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
         }
         __syncthreads();
     }
-    // rotate into the previous eigenvectors, A = C'^T F' C' (W3), and diagonalise
-    qb_cta_gemm(false, false, n, n, n, 1.0, M.W2, n, M.Cp, n, 0.0, M.W1, n);
-    qb_cta_gemm(true, false, n, n, n, 1.0, M.Cp, n, M.W1, n, 0.0, M.W3, n);
-    const int used = qb_cta_jacobi<QB_BATCH_MAXN>(n, M.W3, M.W1, M.Cp, M.eps, M.wt, M.W2, 60, jsm);
-    for (int i = tid; i < nn; i += nt) M.Cp[i] = M.W1[i];
-    __syncthreads();
-    // D' = C'_occ C'_occ^T (W3); D = X D' X^T (W2)
-    qb_cta_gemm(false, true, n, n, M.nocc, 1.0, M.Cp, n, M.Cp, n, 0.0, M.W3, n);
-    qb_cta_gemm(false, false, n, n, n, 1.0, M.X, n, M.W3, n, 0.0, M.W1, n);
-    qb_cta_gemm(false, true, n, n, n, 1.0, M.W1, n, M.X, n, 0.0, M.W2, n);
+    int used = 0;
+    if (prm.eig == 0) {
+        // occupied eigenvectors Y of F' (W1, n x nocc): Householder + bisection + inverse
+        // iteration; D' = Y Y^T (W3) and D = (X Y)(X Y)^T (W2)
+        for (int i = tid; i < nn; i += nt) M.W3[i] = M.W2[i];
+        __syncthreads();
+        qb_cta_lowest_eig<QB_BATCH_MAXN>(n, M.nocc, M.W3, M.W1, M.eps, M.W4, M.W5, M.W6, M.wt, esm);
+        qb_cta_gemm(false, true, n, n, M.nocc, 1.0, M.W1, n, M.W1, n, 0.0, M.W3, n);
+        qb_cta_gemm(false, false, n, M.nocc, n, 1.0, M.X, n, M.W1, n, 0.0, M.W4, n);
+        qb_cta_gemm(false, true, n, n, M.nocc, 1.0, M.W4, n, M.W4, n, 0.0, M.W2, n);
+    } else {
+        // rotate into the previous eigenvectors, A = C'^T F' C' (W3), and diagonalise;
+        // eigenvectors to off(A) <= 1e-12 ||A||: the density they give is exact far below
+        // the 1e-8 density threshold, and the warm start usually needs a single sweep
+        qb_cta_gemm(false, false, n, n, n, 1.0, M.W2, n, M.Cp, n, 0.0, M.W1, n);
+        qb_cta_gemm(true, false, n, n, n, 1.0, M.Cp, n, M.W1, n, 0.0, M.W3, n);
+        used = qb_cta_jacobi<QB_BATCH_MAXN>(n, M.W3, M.W1, M.Cp, M.eps, M.wt, M.W2, prm.sweeps, jsm, 1e-24);
+        for (int i = tid; i < nn; i += nt) M.Cp[i] = M.W1[i];
+        __syncthreads();
+        // D' = C'_occ C'_occ^T (W3); D = X D' X^T (W2)
+        qb_cta_gemm(false, true, n, n, M.nocc, 1.0, M.Cp, n, M.Cp, n, 0.0, M.W3, n);
+        qb_cta_gemm(false, false, n, n, n, 1.0, M.X, n, M.W3, n, 0.0, M.W1, n);
+        qb_cta_gemm(false, true, n, n, n, 1.0, M.W1, n, M.X, n, 0.0, M.W2, n);
+    }
     double dd = 0.0;
     for (int idx = tid; idx < nn; idx += nt) {
         const double d = M.W2[idx] - M.D[idx];
@@ -353,7 +368,7 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
     }
     __syncthreads();
     if (tid == 0) {
-        M.sweeps += used < 0 ? 60 : used;
+        M.sweeps += used < 0 ? prm.sweeps : used;   // Jacobi sweeps (0 with the tridiagonal solver)
         // convergence of the entry of this step (E of D, and D against the density before
         // it), as runHartreeFockCore compares consecutive steps (HartreeFock.jl:1160-1175)
         int conv = 0;
@@ -410,6 +425,8 @@ extern "C" void qb_batch_config_default(qb_batch_config* cfg) {
     cfg->schwarz = 1e-14;
     cfg->iters_per_graph = 4;
     cfg->initial_density = nullptr;
+    cfg->jacobi_sweeps = 0;
+    cfg->eigensolver = 0;
 }
 
 int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nnuc, const double* Z,
@@ -506,7 +523,7 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
         vo[m + 1] = vo[m] + nf[m];
     }
     const long long NN = mo[nmol];
-    const int nmat = 13 + 2 * QB_BATCH_SLOTS;
+    const int nmat = 16 + 2 * QB_BATCH_SLOTS;
     DevArray<double> d_mats, d_vecs, d_B;
     QB_CUDA(ctx, d_mats.ensure((size_t)nmat * NN));
     QB_CUDA(ctx, d_vecs.ensure(2 * (size_t)vo[nmol]));
@@ -518,12 +535,13 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
         std::memset(&M, 0, sizeof(M));
         M.n = nf[m];
         M.nocc = nocc[m];
-        double* mat[13];
-        for (int k = 0; k < 13; ++k) mat[k] = d_mats.p + (size_t)k * NN + mo[m];
+        double* mat[16];
+        for (int k = 0; k < 16; ++k) mat[k] = d_mats.p + (size_t)k * NN + mo[m];
         M.S = mat[0]; M.H = mat[1]; M.X = mat[2]; M.F = mat[3]; M.D = mat[4]; M.Dt = mat[5]; M.Do = mat[6];
         M.Jp = mat[7]; M.Kp = mat[8]; M.Cp = mat[9]; M.W1 = mat[10]; M.W2 = mat[11]; M.W3 = mat[12];
-        M.Fh = d_mats.p + 13 * (size_t)NN + (size_t)QB_BATCH_SLOTS * mo[m];
-        M.Eh = d_mats.p + (13 + QB_BATCH_SLOTS) * (size_t)NN + (size_t)QB_BATCH_SLOTS * mo[m];
+        M.W4 = mat[13]; M.W5 = mat[14]; M.W6 = mat[15];
+        M.Fh = d_mats.p + 16 * (size_t)NN + (size_t)QB_BATCH_SLOTS * mo[m];
+        M.Eh = d_mats.p + (16 + QB_BATCH_SLOTS) * (size_t)NN + (size_t)QB_BATCH_SLOTS * mo[m];
         M.B = d_B.p + (size_t)m * QB_BATCH_SLOTS * QB_BATCH_SLOTS;
         M.eps = d_vecs.p + vo[m];
         M.wt = d_vecs.p + vo[nmol] + vo[m];
@@ -723,7 +741,8 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     QB_CUDA(ctx, d_order.ensure(nmol));
     QB_CUDA(ctx, cudaMemcpyAsync(d_order.p, order.data(), nmol * sizeof(int), cudaMemcpyHostToDevice, s));
     QB_CUDA(ctx, cudaStreamSynchronize(s));
-    const StepParams prm{cfg.conv_energy, cfg.conv_density, cfg.max_iter, cfg.diis_size};
+    const StepParams prm{cfg.conv_energy, cfg.conv_density, cfg.max_iter, cfg.diis_size,
+                         cfg.jacobi_sweeps > 0 ? std::min(cfg.jacobi_sweeps, 60) : 60, cfg.eigensolver ? 1 : 0};
     int* d_active = d_counters.p + 1;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;

@@ -187,6 +187,24 @@ int qb_adjoint_jk(qb_ctx* ctx, const qb_basis* basis, int n, const double* P, do
     return qb_check_status(ctx);
 }
 
+int qb_eigh_lowest(qb_ctx* ctx, int n, int k, const double* A, double* w, double* Y) {
+    QB_TRY(enter(ctx));
+    if (!A || !w || !Y) return qb_set_error(ctx, QB_ERR_ARG, "null argument");
+    if (n < 1 || n > 1024 || k < 1 || k > n) return qb_set_error(ctx, QB_ERR_DIM, "need 1 <= k <= n <= 1024");
+    const size_t nn = (size_t)n * n, nk = (size_t)n * k;
+    QB_CUDA(ctx, ctx->d_m0.ensure(nn));
+    QB_CUDA(ctx, ctx->d_m1.ensure(nk + k + 3 * nk + n));
+    QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_m0.p, A, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    double* dY = ctx->d_m1.p;
+    double* dw = dY + nk;
+    if (qb_lowest_eig(ctx->stream, n, k, ctx->d_m0.p, dY, dw, dw + k) != 0)
+        return qb_cuda_check(ctx, cudaGetLastError(), "eigensolver kernel");
+    QB_CUDA(ctx, cudaMemcpyAsync(Y, dY, nk * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    QB_CUDA(ctx, cudaMemcpyAsync(w, dw, k * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    QB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return QB_OK;
+}
+
 int qb_elec_repulsions(qb_ctx* ctx, const qb_basis* basis, double* eri) {
     QB_TRY(enter(ctx));
     if (!eri) return qb_set_error(ctx, QB_ERR_ARG, "null output");

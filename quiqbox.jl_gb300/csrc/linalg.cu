@@ -69,6 +69,20 @@ __global__ void __launch_bounds__(1024) qb_jacobi_kernel(int n, double* A, doubl
     if (used < 0 && threadIdx.x == 0) atomicOr(status, 2);
 }
 
+// k lowest eigenpairs of a symmetric matrix (the batched SCF's solver) for testing and for
+// callers that need only part of the spectrum; one thread block, n <= 1024.
+__global__ void __launch_bounds__(256) qb_lowest_eig_kernel(int n, int k, double* A, double* Y, double* w,
+                                                            double* B, double* p) {
+    __shared__ QbEigSmem<QB_EIGH_MAXN> sm;
+    qb_cta_lowest_eig<QB_EIGH_MAXN>(n, k, A, Y, w, B, B + (size_t)n * k, B + 2 * (size_t)n * k, p, sm);
+}
+
+int qb_lowest_eig(cudaStream_t s, int n, int k, double* A, double* Y, double* w, double* work) {
+    if (n < 1 || n > QB_EIGH_MAXN || k < 1 || k > n) return -1;
+    qb_lowest_eig_kernel<<<1, 256, 0, s>>>(n, k, A, Y, w, work, work + 3 * (size_t)n * k);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 // w (n), V (n x n) from symmetric A; work needs 2 n^2 + n doubles.
 int qb_eigh(cudaStream_t s, int n, const double* A, double* w, double* V, double* work, int* status) {
     if (n > QB_EIGH_MAXN) return -1;

@@ -59,13 +59,13 @@ struct QbJacobiSmem {
 // rotations are applied to a copy of Vin instead of the identity (V = Vin * rotations:
 // eigenvectors of Vin A Vin^T for orthogonal Vin).  A plane (p, q) is rotated only while
 // |a_pq| > 1e-15 sqrt(|a_pp a_qq|) (below that the rotation changes nothing at double
-// precision); converged when off(A)^2 <= 1e-30 ||A||^2, when a sweep rotated no plane, or
+// precision); converged when off(A)^2 <= tol2 ||A||^2 (default 1e-30), when a sweep rotated no plane, or
 // when off(A)^2 <= 1e-24 ||A||^2 stopped shrinking (rounding level: it fell by less than
 // 4x in the last sweep).  At most maxsweep sweeps; returns the number used, or -1 if not
 // converged (off(A) is then still reported small enough by the caller's own test).
 template <int MAXN>
 __device__ int qb_cta_jacobi(int n, double* A, double* V, const double* Vin, double* w, double* wtmp, double* Vtmp,
-                             int maxsweep, QbJacobiSmem<MAXN>& sm) {
+                             int maxsweep, QbJacobiSmem<MAXN>& sm, double tol2 = 1e-30) {
     const int tid = threadIdx.x, nt = blockDim.x;
     const int m = n + (n & 1);
     const int half = m / 2;
@@ -84,7 +84,7 @@ __device__ int qb_cta_jacobi(int n, double* A, double* V, const double* Vin, dou
         tot = qb_cta_sum(tot, sm.red);
         const int rotated = sm.rotated;   // every thread reads the flag before it is reset
         __syncthreads();
-        if (off <= 1e-30 * tot || off == 0.0 || (sweep > 0 && rotated == 0) ||
+        if (off <= tol2 * tot || off == 0.0 || (sweep > 0 && rotated == 0) ||
             (sweep > 0 && off <= 1e-24 * tot && off > 0.25 * off_prev)) {
             used = sweep;
             break;
@@ -163,4 +163,232 @@ __device__ int qb_cta_jacobi(int n, double* A, double* V, const double* Vin, dou
     for (int i = tid; i < n * n; i += nt) V[i] = Vtmp[i];
     __syncthreads();
     return used;
+}
+
+// ---------------------------------------------------------------------------
+// Lowest eigenpairs of a symmetric matrix by one thread block: Householder
+// tridiagonalisation, FP32 bisection on Sturm counts for the k lowest eigenvalues (the
+// FP32 pipe is ~64x the FP64 one on this GPU), FP64 Rayleigh-quotient inverse iteration
+// with a pivoted tridiagonal LU for the eigenvectors, Gram-Schmidt within clusters of
+// close eigenvalues, and the back-transformation by the stored reflectors.  About
+// (4/3) n^3 + 2 n^2 k FMAs against ~4 n^3 per Jacobi sweep.
+template <int MAXN>
+struct QbEigSmem {
+    double d[MAXN], e[MAXN], lam[MAXN], dots[MAXN];
+    double red[33];
+    double bounds[3];
+};
+
+// A (n x n, column-major, destroyed) -> d, e; reflector k (unit vector, length n-k-1)
+// stored in A[k+1 .. n-1, k].  p is n doubles of scratch.
+template <int MAXN>
+__device__ void qb_cta_tridiag(int n, double* A, double* p, QbEigSmem<MAXN>& sm) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int k = 0; k + 2 < n; ++k) {
+        const int m = n - k - 1;
+        double* x = A + (k + 1) + (size_t)n * k;
+        double s = 0.0;
+        for (int i = tid; i < m; i += nt) s += x[i] * x[i];
+        s = qb_cta_sum(s, sm.red);
+        const double x0 = x[0];
+        const double alpha = (s > 0.0) ? -copysign(sqrt(s), x0) : 0.0;
+        const double vn2 = 2.0 * s - 2.0 * x0 * alpha;
+        const bool refl = s > 0.0 && vn2 > 0.0;
+        if (tid == 0) {
+            sm.d[k] = A[k + (size_t)n * k];
+            sm.e[k] = refl ? alpha : x0;
+        }
+        __syncthreads();   // x0 read by every thread before x is overwritten
+        if (!refl) {
+            for (int i = tid; i < m; i += nt) x[i] = 0.0;
+            __syncthreads();
+            continue;
+        }
+        const double inv = 1.0 / sqrt(vn2);
+        for (int i = tid; i < m; i += nt) x[i] = (i == 0 ? x0 - alpha : x[i]) * inv;
+        __syncthreads();
+        double* S = A + (k + 1) + (size_t)n * (k + 1);
+        for (int i = tid; i < m; i += nt) {
+            double acc = 0.0;
+            for (int j = 0; j < m; ++j) acc = fma(S[i + (size_t)n * j], x[j], acc);
+            p[i] = acc;
+        }
+        double K = 0.0;
+        for (int i = tid; i < m; i += nt) K += x[i] * p[i];
+        K = qb_cta_sum(K, sm.red);
+        for (int i = tid; i < m; i += nt) p[i] -= K * x[i];
+        __syncthreads();
+        for (int idx = tid; idx < m * m; idx += nt) {
+            const int i = idx % m, j = idx / m;
+            S[i + (size_t)n * j] -= 2.0 * (x[i] * p[j] + p[i] * x[j]);
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        if (n >= 2) {
+            sm.d[n - 2] = A[(n - 2) + (size_t)n * (n - 2)];
+            sm.e[n - 2] = A[(n - 1) + (size_t)n * (n - 2)];
+        }
+        sm.d[n - 1] = A[(n - 1) + (size_t)n * (n - 1)];
+    }
+    __syncthreads();
+}
+
+// number of eigenvalues of the tridiagonal (d, e) below x, in FP32 (pivots of the LDL^T
+// factorisation of T - x I; a pivot smaller than `tiny` is replaced by -tiny and counted
+// as negative, which keeps the count consistent when x hits a pivot exactly)
+__device__ __forceinline__ int qb_sturm_f(int n, const double* d, const double* e, float x, float tiny) {
+    float q = (float)d[0] - x;
+    if (fabsf(q) <= tiny) q = -tiny;
+    int c = q < 0.f;
+    for (int j = 1; j < n; ++j) {
+        const float ej = (float)e[j - 1];
+        q = (float)d[j] - x - ej * ej / q;
+        if (fabsf(q) <= tiny) q = -tiny;
+        c += q < 0.f;
+    }
+    return c;
+}
+
+// z = (T - lam I)^{-1} y (T tridiagonal d, e) by Gaussian elimination with partial pivoting;
+// u0, u1, u2 (n each, strided by `ld` like y) are the rows of U.  y is overwritten by z.
+static __device__ void qb_tridiag_solve(int n, const double* d, const double* e, double lam, double pert, double* y,
+                                        double* u0, double* u1, double* u2, int ld) {
+    double m0 = d[0] - lam, m1 = n > 1 ? e[0] : 0.0, m2 = 0.0;
+    for (int j = 0; j + 1 < n; ++j) {
+        const double l = e[j], a = d[j + 1] - lam, b = (j + 2 < n) ? e[j + 1] : 0.0;
+        const double rj = y[(size_t)ld * j], rn = y[(size_t)ld * (j + 1)];
+        if (fabs(l) > fabs(m0)) {
+            const double f = m0 / l;
+            u0[(size_t)ld * j] = l;
+            u1[(size_t)ld * j] = a;
+            u2[(size_t)ld * j] = b;
+            y[(size_t)ld * j] = rn;
+            y[(size_t)ld * (j + 1)] = rj - f * rn;
+            m0 = m1 - f * a;
+            m1 = m2 - f * b;
+            m2 = 0.0;
+        } else {
+            if (m0 == 0.0) m0 = pert;
+            const double f = l / m0;
+            u0[(size_t)ld * j] = m0;
+            u1[(size_t)ld * j] = m1;
+            u2[(size_t)ld * j] = m2;
+            y[(size_t)ld * (j + 1)] = rn - f * rj;
+            m0 = a - f * m1;
+            m1 = b - f * m2;
+            m2 = 0.0;
+        }
+    }
+    if (m0 == 0.0) m0 = pert;
+    u0[(size_t)ld * (n - 1)] = m0;
+    for (int j = n - 1; j >= 0; --j) {
+        double s = y[(size_t)ld * j];
+        if (j + 1 < n) s -= u1[(size_t)ld * j] * y[(size_t)ld * (j + 1)];
+        if (j + 2 < n) s -= u2[(size_t)ld * j] * y[(size_t)ld * (j + 2)];
+        y[(size_t)ld * j] = s / u0[(size_t)ld * j];
+    }
+}
+
+// k lowest eigenpairs of the symmetric n x n matrix A (destroyed): eigenvalues in w[0..k),
+// eigenvectors in the columns of Y (n x k, column-major).  B0, B1, B2 are n x k scratch
+// (band rows of the inverse-iteration LU) and p n doubles of scratch.
+template <int MAXN>
+__device__ void qb_cta_lowest_eig(int n, int k, double* A, double* Y, double* w, double* B0, double* B1, double* B2,
+                                  double* p, QbEigSmem<MAXN>& sm) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    qb_cta_tridiag<MAXN>(n, A, p, sm);
+    if (tid == 0) {   // Gershgorin interval and the scale of T
+        double lo = 0.0, hi = 0.0;
+        for (int i = 0; i < n; ++i) {
+            const double r = (i > 0 ? fabs(sm.e[i - 1]) : 0.0) + (i + 1 < n ? fabs(sm.e[i]) : 0.0);
+            lo = (i == 0) ? sm.d[i] - r : fmin(lo, sm.d[i] - r);
+            hi = (i == 0) ? sm.d[i] + r : fmax(hi, sm.d[i] + r);
+        }
+        const double nrm = fmax(fabs(lo), fabs(hi)) + 1e-300;
+        sm.bounds[0] = lo - 1e-6 * nrm;
+        sm.bounds[1] = hi + 1e-6 * nrm;
+        sm.bounds[2] = nrm;
+    }
+    __syncthreads();
+    const double nrm = sm.bounds[2];
+    const double pert = 1e-16 * nrm;
+    // eigenvalue i by FP32 bisection, refined by FP64 Rayleigh-quotient inverse iteration
+    for (int i = tid; i < k; i += nt) {
+        float lo = (float)sm.bounds[0], hi = (float)sm.bounds[1];
+        const float tiny = (float)(1e-30 * nrm) + 1e-30f;
+        for (int it = 0; it < 64; ++it) {
+            const float mid = 0.5f * (lo + hi);
+            if (!(mid > lo && mid < hi)) break;
+            if (qb_sturm_f(n, sm.d, sm.e, mid, tiny) > i) hi = mid;
+            else lo = mid;
+        }
+        const double lam = 0.5 * ((double)lo + (double)hi);
+        double* y = Y + (size_t)n * i;
+        for (int j = 0; j < n; ++j) {   // deterministic start vector, distinct per eigenvalue
+            const unsigned h = (unsigned)(j * 2654435761u) ^ (unsigned)(i * 40503u + 17u);
+            y[j] = 1.0 + 0.25 * ((double)(h & 0xffff) / 65536.0 - 0.5);
+        }
+        // inverse iteration at the fixed FP32 shift (within ~1e-7 ||T|| of the eigenvalue):
+        // components of eigenvalues further than 1e-4 ||T|| shrink by >= 1e3 per step
+        for (int s = 0; s < 6; ++s) {
+            qb_tridiag_solve(n, sm.d, sm.e, lam, pert, y, B0 + (size_t)n * i, B1 + (size_t)n * i,
+                             B2 + (size_t)n * i, 1);
+            double nn2 = 0.0;
+            for (int j = 0; j < n; ++j) nn2 += y[j] * y[j];
+            const double inv = 1.0 / sqrt(nn2);
+            for (int j = 0; j < n; ++j) y[j] *= inv;
+        }
+        sm.lam[i] = lam;
+    }
+    __syncthreads();
+    // Gram-Schmidt within clusters (|lam_i - lam_j| <= 1e-4 ||T||: the eigenvalues inverse
+    // iteration cannot separate), normalisation
+    for (int i = 0; i < k; ++i) {
+        double* yi = Y + (size_t)n * i;
+        for (int j = 0; j < i; ++j) {
+            if (fabs(sm.lam[i] - sm.lam[j]) > 1e-4 * nrm) continue;
+            const double* yj = Y + (size_t)n * j;
+            double dot = 0.0;
+            for (int r = tid; r < n; r += nt) dot += yi[r] * yj[r];
+            dot = qb_cta_sum(dot, sm.red);
+            for (int r = tid; r < n; r += nt) yi[r] -= dot * yj[r];
+            __syncthreads();
+        }
+        double nn2 = 0.0;
+        for (int r = tid; r < n; r += nt) nn2 += yi[r] * yi[r];
+        nn2 = qb_cta_sum(nn2, sm.red);
+        const double inv = 1.0 / sqrt(nn2);
+        for (int r = tid; r < n; r += nt) yi[r] *= inv;
+        __syncthreads();
+    }
+    for (int i = tid; i < k; i += nt) {   // eigenvalue = Rayleigh quotient of the final vector
+        const double* y = Y + (size_t)n * i;
+        double rq = 0.0;
+        for (int j = 0; j < n; ++j) {
+            double ty = sm.d[j] * y[j];
+            if (j > 0) ty += sm.e[j - 1] * y[j - 1];
+            if (j + 1 < n) ty += sm.e[j] * y[j + 1];
+            rq += y[j] * ty;
+        }
+        w[i] = rq;
+    }
+    __syncthreads();
+    // back-transformation: Y <- H_0 H_1 ... H_{n-3} Y
+    for (int kk = n - 3; kk >= 0; --kk) {
+        const int m = n - kk - 1;
+        const double* v = A + (kk + 1) + (size_t)n * kk;
+        for (int c = tid; c < k; c += nt) {
+            const double* yc = Y + (size_t)n * c + kk + 1;
+            double dot = 0.0;
+            for (int r = 0; r < m; ++r) dot = fma(v[r], yc[r], dot);
+            sm.dots[c] = dot;
+        }
+        __syncthreads();
+        for (int idx = tid; idx < m * k; idx += nt) {
+            const int r = idx % m, c = idx / m;
+            Y[(size_t)n * c + kk + 1 + r] -= 2.0 * v[r] * sm.dots[c];
+        }
+        __syncthreads();
+    }
 }

@@ -85,6 +85,7 @@ int qb_build_prim_pairs(cudaStream_t s, const PairSlot* d_slots, int nslot, cons
                         PrimPair* d_prims, float4* d_prims32, int* d_nkept, unsigned long long* d_kmax);
 
 int qb_jk_autotune_device(qb_ctx* ctx, int repeats, int* chosen);
+int qb_lowest_eig(cudaStream_t s, int n, int k, double* A, double* Y, double* w, double* work);
 int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nnuc, const double* Z,
                      const double* R, const int* nocc, const qb_batch_config* cfg, qb_batch_result* res);
 
