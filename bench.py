@@ -433,8 +433,9 @@ def batched_rhf(qb, n_mol, seed, cpu_seconds):
            "wall_s": wall, "ms_integrals": res.ms_integrals, "ms_scf": res.ms_scf,
            "mean_iterations_converged": float(res.iterations[conv].mean()) if conv.any() else None,
            "graph_launches": res.graph_launches, "stored_quartets": res.quartets,
-           "stored_eri_gb": res.eri_doubles * 8 / 1e9, "mean_jacobi_sweeps_per_iteration":
-           float((res.jacobi_sweeps / np.maximum(res.iterations, 1)).mean())}
+           "stored_eri_gb": res.eri_doubles * 8 / 1e9,
+           "eigensolver": "occupied subspace: Householder tridiagonalisation, FP32 Sturm bisection, "
+                          "FP64 inverse iteration (one thread block per molecule)"}
     # CPU baseline: the oracle's RHF (the reference's algorithm, DIIS only) on random molecules
     rng = np.random.default_rng(seed + 17)
     order = rng.permutation(n_mol)

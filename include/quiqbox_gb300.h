@@ -107,6 +107,22 @@ int qb_mse_grad(int64_t n, const float* y, const float* t, const float* w, float
 int qb_adam_step(int64_t n, float* w, const float* g, float* m, float* v, void* w_bf16, float lr, float b1, float b2,
                  float eps, int step, void* stream);
 
+/* Learned guess inputs and outputs on the device (one thread per atom pair (a, b), a <= b,
+ * global atom indices; molecule m owns atoms [mol_atom0[m], mol_atom0[m] + mol_natom[m]);
+ * atom_el: 0 H, 1 C, 2 N, 3 O; minimal basis, functions 1s (H) or 1s 2s 2px 2py 2pz).
+ * qb_guess_features: X (npair x 128 fp32, row-major) = the pair's network input, R
+ *   (npair x 9, row-major 3 x 3) = its local frame (columns: local x, y, z axes).
+ * qb_guess_assemble: per-spin densities D (column-major, molecule m at D + mol_off[m],
+ *   mol_n[m] x mol_n[m]) from the network's local-frame 5 x 5 blocks Y (row p, leading
+ *   dimension ldy >= 25): block (a, b) = T Y_p T^T with T = diag(1, 1, R_p), written to
+ *   the (a, b) and (b, a) blocks; atom_f0 = first function of each atom in its molecule. */
+int qb_guess_features(int npair, const int* pair_mol, const int* pair_a, const int* pair_b, const int* mol_atom0,
+                      const int* mol_natom, const double* atom_pos, const int* atom_el, const float* mol_charge,
+                      float* X, double* R, void* stream);
+int qb_guess_assemble(int npair, const int* pair_mol, const int* pair_a, const int* pair_b, const int* atom_el,
+                      const int* atom_f0, const long long* mol_off, const int* mol_n, const float* Y, int ldy,
+                      const double* R, double* D, void* stream);
+
 /* Backward pass of the two-electron energy for basis-parameter gradients (the reference
  * has no analytic gradient; src/Differentiation/Finite.jl holds finite-difference
  * weights only).  Functions [0, n) of `basis` are the basis, [n, nfun) extra single
@@ -227,11 +243,16 @@ typedef struct {
     double schwarz;         /* stored-integral screening Q_ab Q_cd >= schwarz, default 1e-14 */
     int iters_per_graph;    /* SCF iterations per CUDA-graph launch, default 4 */
     const double* initial_density;  /* NULL: core-Hamiltonian guess; else per-spin densities
-                                       of all molecules, nfun x nfun each, concatenated */
+                                       of all molecules, nfun x nfun each (column-major),
+                                       concatenated; host or device memory */
     int eigensolver;        /* 0 (default): occupied eigenvectors by Householder tridiagonalisation,
                                bisection and inverse iteration; 1: Jacobi over all eigenvectors */
     int jacobi_sweeps;      /* eigensolver 1: sweeps per SCF iteration (eigenvectors carry over from
                                the previous iteration); 0: until converged (default) */
+    int fallback_iter;      /* with initial_density: a molecule not converged after this many
+                               iterations restarts from the core-Hamiltonian guess in the same call
+                               (the iterations of both attempts count against max_iter); 0: never
+                               (default) */
 } qb_batch_config;
 
 typedef struct {
@@ -246,6 +267,7 @@ typedef struct {
     int64_t eri_doubles;    /* stored integrals */
     int graph_launches;
     double* density;        /* NULL or room for the final per-spin densities, concatenated */
+    int* restarted;         /* NULL or nmol: 1 if the molecule restarted from the core-Hamiltonian guess */
 } qb_batch_result;
 
 void qb_batch_config_default(qb_batch_config* cfg);

@@ -23,7 +23,8 @@ EXPORTED = ["qb_create", "qb_destroy", "qb_last_error", "qb_device_info", "qb_ov
             "qb_scf_config_default", "qb_run_hartree_fock", "qb_fp64_peak", "qb_jk_noalloc", "qb_boys", "qb_multipole_moments",
             "qb_batch_config_default", "qb_run_rhf_batched", "qb_jk_autotune",
             "qb_bf16_gemm_nt", "qb_gelu_forward", "qb_gelu_backward", "qb_f32_to_bf16", "qb_bf16_transpose",
-            "qb_colsum", "qb_mse_grad", "qb_adam_step", "qb_adjoint_jk", "qb_eigh_lowest"]
+            "qb_colsum", "qb_mse_grad", "qb_adam_step", "qb_adjoint_jk", "qb_eigh_lowest",
+            "qb_guess_features", "qb_guess_assemble"]
 
 
 class DimensionMismatch(ValueError):
@@ -166,7 +167,8 @@ class Context:
 class QBBatchConfig(C.Structure):
     _fields_ = [("conv_energy", C.c_double), ("conv_density", C.c_double), ("max_iter", C.c_int),
                 ("diis_size", C.c_int), ("schwarz", C.c_double), ("iters_per_graph", C.c_int),
-                ("initial_density", C.POINTER(C.c_double)), ("eigensolver", C.c_int), ("jacobi_sweeps", C.c_int)]
+                ("initial_density", C.POINTER(C.c_double)), ("eigensolver", C.c_int), ("jacobi_sweeps", C.c_int),
+                ("fallback_iter", C.c_int)]
 
 
 class QBBatchResult(C.Structure):
@@ -174,7 +176,7 @@ class QBBatchResult(C.Structure):
                 ("converged", C.POINTER(C.c_int)), ("jacobi_sweeps", C.POINTER(C.c_int)),
                 ("ms_integrals", C.c_double), ("ms_scf", C.c_double), ("quartets", C.c_int64),
                 ("prim_quartets", C.c_int64), ("eri_doubles", C.c_int64), ("graph_launches", C.c_int),
-                ("density", C.POINTER(C.c_double))]
+                ("density", C.POINTER(C.c_double)), ("restarted", C.POINTER(C.c_int))]
 
 
 class BasisArgs:

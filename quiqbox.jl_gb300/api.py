@@ -345,6 +345,11 @@ def computeBoysFunc(T, m, ctx=None):
     return float(computeBoysSequence(np.array([T]), m, path=1 if m > 8 else 0, ctx=ctx)[0, m])
 
 
+def _torch_float64():
+    import torch
+    return torch.float64
+
+
 @dataclass
 class BatchSCFConfig:
     """Configuration of runHartreeFockBatched (qb_batch_config)."""
@@ -356,6 +361,7 @@ class BatchSCFConfig:
     iters_per_graph: int = 4
     eigensolver: int = 0          # 0: tridiagonal occupied-subspace solver; 1: Jacobi
     jacobi_sweeps: int = 0        # Jacobi sweeps per SCF iteration; 0 = to convergence
+    fallback_iter: int = 0        # with initial densities: restart from CoreH after this many iterations
 
 
 @dataclass
@@ -373,6 +379,7 @@ class BatchSCFResult:
     eri_doubles: int
     graph_launches: int
     densities: Optional[list] = None   # final per-spin densities (return_densities=True)
+    restarted: Optional[np.ndarray] = None   # restarted from the core-Hamiltonian guess (fallback_iter)
 
 
 def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ctx=None,
@@ -408,7 +415,14 @@ def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ct
     R = np.ascontiguousarray(np.concatenate(Rs), np.float64)
     nocc_a = np.ascontiguousarray(nocc, np.int32)
     d0 = None
-    if initial_densities is not None:
+    d0_dev = None
+    if initial_densities is not None and hasattr(initial_densities, "data_ptr"):
+        # one float64 device (or host) tensor: all molecules' column-major densities, concatenated
+        if initial_densities.dtype != _torch_float64() or initial_densities.numel() < sum(n * n for n in nf) \
+                or not initial_densities.is_contiguous():
+            raise DimensionMismatch("initial density tensor: contiguous float64 with sum(nfun^2) entries")
+        d0_dev = C.cast(initial_densities.data_ptr(), C.POINTER(C.c_double))
+    elif initial_densities is not None:
         if len(initial_densities) != nmol:
             raise DimensionMismatch("one initial density per molecule")
         parts = []
@@ -419,15 +433,16 @@ def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ct
             parts.append(D.reshape(-1, order="F"))
         d0 = np.ascontiguousarray(np.concatenate(parts))
     qcfg = L.QBBatchConfig(cfg.conv_energy, cfg.conv_density, cfg.max_iter, cfg.diis_size, cfg.schwarz,
-                           cfg.iters_per_graph, L.dptr(d0) if d0 is not None else None, cfg.eigensolver,
-                           cfg.jacobi_sweeps)
+                           cfg.iters_per_graph, L.dptr(d0) if d0 is not None else d0_dev, cfg.eigensolver,
+                           cfg.jacobi_sweeps, cfg.fallback_iter)
     E = np.zeros(nmol)
     it = np.zeros(nmol, np.int32)
     conv = np.zeros(nmol, np.int32)
     sw = np.zeros(nmol, np.int32)
     dout = np.zeros(sum(n * n for n in nf)) if return_densities else None
+    rst = np.zeros(nmol, np.int32)
     res = L.QBBatchResult(L.dptr(E), L.iptr(it), L.iptr(conv), L.iptr(sw), 0.0, 0.0, 0, 0, 0, 0,
-                          L.dptr(dout) if dout is not None else None)
+                          L.dptr(dout) if dout is not None else None, L.iptr(rst))
     c.check(c.lib.qb_run_rhf_batched(c.h, nmol, bases, L.iptr(nnuc_a), L.dptr(Z), L.dptr(R), L.iptr(nocc_a),
                                      C.byref(qcfg), C.byref(res)))
     dens = None
@@ -438,7 +453,7 @@ def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ct
             off += n * n
     return BatchSCFResult(E + np.array(enn), E, it, conv.astype(bool), sw, np.array(nf), res.ms_integrals,
                           res.ms_scf, int(res.quartets), int(res.prim_quartets), int(res.eri_doubles),
-                          int(res.graph_launches), dens)
+                          int(res.graph_launches), dens, rst.astype(bool))
 
 
 def fp64_peak(ctx=None):

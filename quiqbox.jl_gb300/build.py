@@ -21,7 +21,7 @@ OBJ = OUT / "obj"
 INCLUDE = PKG.parent / "include"
 LIB = OUT / "libquiqbox_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-HAND_WRITTEN = ["engine.cu", "generic.cu", "linalg.cu", "scf.cu", "capi.cu", "noalloc.cu", "batch.cu", "mlp.cu"]
+HAND_WRITTEN = ["engine.cu", "generic.cu", "linalg.cu", "scf.cu", "capi.cu", "noalloc.cu", "batch.cu", "mlp.cu", "guess.cu"]
 
 
 def _nvcc():

@@ -58,9 +58,20 @@ struct BatchWork {           // one class: quartets t in [0, offs[nbra])
     int same;                // X == Y
 };
 
+// A contiguous range of one class's stored quartets, all of one molecule (bra pairs are
+// sorted by molecule, and every bra's kets lie in its own molecule): the digest of an
+// iteration visits a chunk only while its molecule iterates.
+struct DigestChunk {
+    long long t0, t1;        // quartets [t0, t1)
+    int b0, b1;              // bras [b0, b1) own them (offs[b0] <= t0, offs[b1] >= t1)
+    int mol, pad;
+};
+#define QB_DIGEST_CHUNK 2048
+
 struct MolDev {
     int n, nocc, conv, iter;   // conv: 0 iterating, 1 converged, 2 stopped at max_iter, 3 failed
     int dlen, sweeps;          // DIIS subspace: dlist[0..dlen) slot ids, oldest first
+    int iter0, restarted;      // iterations before a restart from the core-Hamiltonian guess
     int dlist[QB_BATCH_SLOTS];
     double dEs[QB_BATCH_SLOTS];   // per-spin energy of each slot's entry
     double E, Eprev, dE, rmsD;
@@ -72,6 +83,7 @@ struct MolDev {
 struct StepParams {
     double thr_e, thr_d;
     int max_iter, diis, sweeps, eig;   // eig 0: tridiagonal occupied-subspace solver, 1: Jacobi
+    int fallback;                      // > 0: restart from the core-Hamiltonian guess after this many
 };
 
 // ---------------------------------------------------------------------------
@@ -99,26 +111,60 @@ __global__ void __launch_bounds__(128) qb_batch_store_kernel(const BatchWork w, 
     if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(primcount, cnt);
 }
 
+// One thread block per chunk; the blocks of converged molecules return after one read.
 template <int LA, int LB, int LC, int LD>
-__global__ void __launch_bounds__(128) qb_batch_digest_kernel(const BatchWork w, const double* __restrict__ in,
+__global__ void __launch_bounds__(128) qb_batch_digest_kernel(const BatchWork w, const DigestChunk* __restrict__ chunks,
+                                                              const double* __restrict__ in,
                                                               const MolDev* __restrict__ mols) {
     using C = EriClass<LA, LB, LC, LD>;
+    const DigestChunk ch = chunks[blockIdx.x];
+    const MolDev& M = mols[ch.mol];
+    if (M.conv) return;
     const long long total = __ldg(w.offs + w.nbra);
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
-        const int i = qb_find_bra(w.offs, w.nbra, t);
+    const JKArgs a{nullptr, nullptr, nullptr, M.Dt, M.Jp, M.Kp, nullptr, M.n};
+    for (long long t = ch.t0 + threadIdx.x; t < ch.t1; t += blockDim.x) {
+        int i = ch.b0, hi = ch.b1;   // largest i in [b0, b1) with offs[i] <= t
+        while (hi - i > 1) {
+            const int mid = (i + hi) >> 1;
+            if (__ldg(w.offs + mid) <= t) i = mid; else hi = mid;
+        }
         const int j = __ldg(w.kstart + i) + (int)(t - __ldg(w.offs + i));
         const ShellPair P = w.bra[i];
-        const MolDev& M = mols[P.pad];
-        if (M.conv) continue;
         const ShellPair Q = w.ket[j];
         double I[C::NINT];
 #pragma unroll
         for (int k = 0; k < C::NINT; ++k) I[k] = __ldg(in + (size_t)k * total + t);
-        const JKArgs a{nullptr, nullptr, nullptr, M.Dt, M.Jp, M.Kp, nullptr, M.n};
         const double deg = (P.same ? 1.0 : 2.0) * (Q.same ? 1.0 : 2.0) * ((w.same && i == j) ? 1.0 : 2.0);
         qb_jk_digest<C>(P, Q, deg, a, I);
     }
+}
+
+// Schwarz factors Q_ab = max over components sqrt|(ab|ab)| of one pair class, from the
+// class's own primitive-pair quartet code (the shell integrals times the per-function
+// ratios r_a r_b of the basis weights).
+template <int LA, int LB>
+__global__ void __launch_bounds__(128) qb_batch_schwarz_kernel(const ShellPair* __restrict__ pairs, int n,
+                                                               const PrimPair* __restrict__ prims,
+                                                               const double* __restrict__ boys,
+                                                               const double* __restrict__ ratio,
+                                                               double* __restrict__ Q) {
+    using C = EriClass<LA, LB, LA, LB>;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const ShellPair P = pairs[k];
+    double I[C::NINT];
+    unsigned cnt = 0;
+    C::block(prims + P.prim0, P.nprim, prims + P.prim0, P.nprim, P.ABx, P.ABy, P.ABz, P.ABx, P.ABy, P.ABz, boys, I,
+             cnt);
+    double mx = 0.0;
+#pragma unroll
+    for (int x = 0; x < C::NA; ++x)
+#pragma unroll
+        for (int y = 0; y < C::NB; ++y) {
+            const double r = __ldg(ratio + P.fa + x) * __ldg(ratio + P.fb + y);
+            mx = fmax(mx, fabs(I[((x * C::NB + y) * C::NA + x) * C::NB + y]) * r * r);
+        }
+    Q[k] = sqrt(mx);
 }
 
 // X = S^{-1/2} by the eigen-decomposition of S; C' = I; D = D' = 0, or with an initial
@@ -234,7 +280,12 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
     const double* r = M.ratio;
     double E = 0.0;
     if (it == 0) {
-        for (int i = tid; i < nn; i += nt) M.F[i] = M.H[i];
+        // core-Hamiltonian guess (also after a restart: drop what the digest accumulated)
+        for (int i = tid; i < nn; i += nt) {
+            M.F[i] = M.H[i];
+            M.Jp[i] = 0.0;
+            M.Kp[i] = 0.0;
+        }
         __syncthreads();
     } else {
         // F = H + 2J - K (libint-convention accumulators, per-function ratios), energy of D
@@ -283,17 +334,18 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
         }
         __syncthreads();
         const int len0 = M.dlen;
-        for (int k = 0; k <= len0; ++k) {
+        for (int k = tid >> 5; k <= len0; k += nt >> 5) {   // one warp per Gram-matrix entry
             const int other = (k < len0) ? M.dlist[k] : slot;
             const double* Ek = M.Eh + (size_t)other * nn;
             double dot = 0.0;
-            for (int idx = tid; idx < nn; idx += nt) dot += Es[idx] * Ek[idx];
-            dot = qb_cta_sum(dot, red);
-            if (tid == 0) {
+            for (int idx = tid & 31; idx < nn; idx += 32) dot = fma(Es[idx], Ek[idx], dot);
+            dot = qb_group_sum(dot, 32);
+            if ((tid & 31) == 0) {
                 M.B[slot * QB_BATCH_SLOTS + other] = dot;
                 M.B[other * QB_BATCH_SLOTS + slot] = dot;
             }
         }
+        __syncthreads();
         if (tid == 0) {
             M.dEs[slot] = 0.5 * E;   // per-spin energy of the entry
             M.dlist[M.dlen++] = slot;
@@ -380,7 +432,17 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
         }
         M.rmsD = rms;   // change of the density handed to the next step
         M.iter = it + 1;
-        if (!conv && M.iter >= prm.max_iter) conv = 2;
+        const int spent = M.iter0 + M.iter;
+        if (!conv && prm.fallback > 0 && !M.restarted && M.iter >= prm.fallback && spent < prm.max_iter) {
+            // the supplied initial density has not converged: start again from F = H with an
+            // empty DIIS subspace (the next step ignores D and the J'/K' of this iteration)
+            M.iter0 = spent;
+            M.iter = 0;
+            M.dlen = 0;
+            M.restarted = 1;
+        } else if (!conv && spent >= prm.max_iter) {
+            conv = 2;
+        }
         M.conv = conv;
         if (!conv) atomicAdd(active, 1);
     }
@@ -392,14 +454,15 @@ void launch_store(const BatchWork& w, const PrimPair* prims, const double* boys,
     qb_batch_store_kernel<LA, LB, LC, LD><<<grid, 128, 0, s>>>(w, prims, boys, out, pc);
 }
 template <int LA, int LB, int LC, int LD>
-void launch_digest(const BatchWork& w, const double* in, const MolDev* mols, int grid, cudaStream_t s) {
-    qb_batch_digest_kernel<LA, LB, LC, LD><<<grid, 128, 0, s>>>(w, in, mols);
+void launch_digest(const BatchWork& w, const DigestChunk* chunks, const double* in, const MolDev* mols, int grid,
+                   cudaStream_t s) {
+    qb_batch_digest_kernel<LA, LB, LC, LD><<<grid, 128, 0, s>>>(w, chunks, in, mols);
 }
 
 struct ClassDef {
     int la, lb, lc, ld, nint;
     void (*store)(const BatchWork&, const PrimPair*, const double*, double*, unsigned long long*, int, cudaStream_t);
-    void (*digest)(const BatchWork&, const double*, const MolDev*, int, cudaStream_t);
+    void (*digest)(const BatchWork&, const DigestChunk*, const double*, const MolDev*, int, cudaStream_t);
 };
 
 const ClassDef kClasses[QB_BATCH_NCLASS] = {
@@ -427,6 +490,7 @@ extern "C" void qb_batch_config_default(qb_batch_config* cfg) {
     cfg->initial_density = nullptr;
     cfg->jacobi_sweeps = 0;
     cfg->eigensolver = 0;
+    cfg->fallback_iter = 0;
 }
 
 int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nnuc, const double* Z,
@@ -437,6 +501,7 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     if (cfg_in) cfg = *cfg_in;
     else qb_batch_config_default(&cfg);
     if (cfg.diis_size < 1 || cfg.diis_size > QB_BATCH_DIIS || cfg.max_iter < 1 || cfg.iters_per_graph < 1 ||
+        cfg.fallback_iter < 0 ||
         !(cfg.schwarz >= 0.0) || !(cfg.conv_energy > 0.0) || !(cfg.conv_density > 0.0))
         return qb_set_error(ctx, QB_ERR_DOMAIN, "bad batched SCF configuration");
     cudaStream_t s = ctx->stream;
@@ -640,12 +705,15 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
         QB_CUDA(ctx, cudaMemcpyAsync(d_pairs.p, pairs.data(), npair * sizeof(ShellPair), cudaMemcpyHostToDevice, s));
     }
     for (int pc = 0; pc < npc; ++pc) {
-        const int la = pc == 0 ? 0 : 1, lb = pc == 2 ? 1 : 0;
         const int n = pc_off[pc + 1] - pc_off[pc];
         if (n == 0) continue;
-        if (qb_gen_schwarz(gb, ctx->boys.p, d_pairs.p + pc_off[pc], n, (la + 1) * (la + 2) / 2,
-                           (lb + 1) * (lb + 2) / 2, d_Q.p + pc_off[pc], ctx->status.p, s) != 0)
-            return qb_cuda_check(ctx, cudaGetLastError(), "batched Schwarz kernel");
+        const ShellPair* pp = d_pairs.p + pc_off[pc];
+        double* q = d_Q.p + pc_off[pc];
+        const int g = (n + 127) / 128;
+        if (pc == 0) qb_batch_schwarz_kernel<0, 0><<<g, 128, 0, s>>>(pp, n, d_prims.p, ctx->boys.p, d_ratio.p, q);
+        else if (pc == 1) qb_batch_schwarz_kernel<1, 0><<<g, 128, 0, s>>>(pp, n, d_prims.p, ctx->boys.p, d_ratio.p, q);
+        else qb_batch_schwarz_kernel<1, 1><<<g, 128, 0, s>>>(pp, n, d_prims.p, ctx->boys.p, d_ratio.p, q);
+        QB_CUDA(ctx, cudaGetLastError());
     }
     QB_TRY(qb_check_status(ctx));
     {
@@ -723,13 +791,38 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
         cd.store(work[c], d_prims.p, ctx->boys.p, d_eri.p + eri_at[c], d_primcount.p, grid, s);
     }
     QB_CUDA(ctx, cudaGetLastError());
+    // ---- digest chunks: per class and molecule, runs of at most QB_DIGEST_CHUNK quartets
+    std::vector<DigestChunk> h_chunks;
+    std::vector<size_t> chunk_at(QB_BATCH_NCLASS + 1, 0);
+    for (int c = 0; c < QB_BATCH_NCLASS; ++c) {
+        chunk_at[c] = h_chunks.size();
+        const ClassDef& cd = kClasses[c];
+        const int X = pc_of(cd.la, cd.lb);
+        const long long* off = h_offs.data() + offs_at[c];
+        for (int m = 0; m < nmol; ++m) {
+            const int s0 = seg[X][m], s1 = seg[X][m + 1];
+            for (long long t0 = off[s0]; t0 < off[s1]; t0 += QB_DIGEST_CHUNK) {
+                const long long t1 = std::min<long long>(t0 + QB_DIGEST_CHUNK, off[s1]);
+                // bras owning [t0, t1): largest b with off[b] <= t0, one past the largest with off[b] <= t1 - 1
+                const int b0 = (int)(std::upper_bound(off + s0, off + s1, t0) - off) - 1;
+                const int b1 = (int)(std::upper_bound(off + s0, off + s1, t1 - 1) - off);
+                h_chunks.push_back(DigestChunk{t0, t1, b0, b1, m, 0});
+            }
+        }
+    }
+    chunk_at[QB_BATCH_NCLASS] = h_chunks.size();
+    DevArray<DigestChunk> d_chunks;
+    QB_CUDA(ctx, d_chunks.ensure(std::max<size_t>(1, h_chunks.size())));
+    if (!h_chunks.empty())
+        QB_CUDA(ctx, cudaMemcpyAsync(d_chunks.p, h_chunks.data(), h_chunks.size() * sizeof(DigestChunk),
+                                     cudaMemcpyHostToDevice, s));
     // ---- X = S^{-1/2}
     DevArray<int> d_counters;   // [0] failed, [1] active
     QB_CUDA(ctx, d_counters.ensure(2));
     QB_CUDA(ctx, cudaMemsetAsync(d_counters.p, 0, 2 * sizeof(int), s));
     if (cfg.initial_density)
         QB_CUDA(ctx, cudaMemcpyAsync(d_mats.p + 4 * (size_t)NN, cfg.initial_density, NN * sizeof(double),
-                                     cudaMemcpyHostToDevice, s));
+                                     cudaMemcpyDefault, s));   // host or device memory
     qb_batch_orth_kernel<<<nmol, QB_BATCH_THREADS, 0, s>>>(d_mols.p, d_counters.p, cfg.initial_density ? 1 : 0);
     QB_CUDA(ctx, cudaGetLastError());
     QB_CUDA(ctx, cudaEventRecord(ev1, s));
@@ -742,7 +835,8 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     QB_CUDA(ctx, cudaMemcpyAsync(d_order.p, order.data(), nmol * sizeof(int), cudaMemcpyHostToDevice, s));
     QB_CUDA(ctx, cudaStreamSynchronize(s));
     const StepParams prm{cfg.conv_energy, cfg.conv_density, cfg.max_iter, cfg.diis_size,
-                         cfg.jacobi_sweeps > 0 ? std::min(cfg.jacobi_sweeps, 60) : 60, cfg.eigensolver ? 1 : 0};
+                         cfg.jacobi_sweeps > 0 ? std::min(cfg.jacobi_sweeps, 60) : 60, cfg.eigensolver ? 1 : 0,
+                         cfg.initial_density && cfg.fallback_iter > 0 ? cfg.fallback_iter : 0};
     int* d_active = d_counters.p + 1;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -750,9 +844,9 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     for (int k = 0; k < cfg.iters_per_graph; ++k) {
         cudaMemsetAsync(d_active, 0, sizeof(int), s);
         for (int c = 0; c < QB_BATCH_NCLASS; ++c) {
-            if (total[c] == 0) continue;
-            const int grid = (int)std::min<long long>((total[c] + 127) / 128, (long long)ctx->nsm * 16);
-            kClasses[c].digest(work[c], d_eri.p + eri_at[c], d_mols.p, grid, s);
+            const int nch = (int)(chunk_at[c + 1] - chunk_at[c]);
+            if (nch == 0) continue;
+            kClasses[c].digest(work[c], d_chunks.p + chunk_at[c], d_eri.p + eri_at[c], d_mols.p, nch, s);
         }
         qb_batch_step_kernel<<<nmol, QB_BATCH_THREADS, 0, s>>>(d_mols.p, d_order.p, prm, d_active);
     }
@@ -799,7 +893,8 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     int failed = 0;
     for (int m = 0; m < nmol; ++m) {
         if (res->energy) res->energy[m] = hm[m].E;
-        if (res->iterations) res->iterations[m] = hm[m].iter;
+        if (res->iterations) res->iterations[m] = hm[m].iter0 + hm[m].iter;
+        if (res->restarted) res->restarted[m] = hm[m].restarted;
         if (res->converged) res->converged[m] = hm[m].conv == 1 ? 1 : 0;
         if (res->jacobi_sweeps) res->jacobi_sweeps[m] = hm[m].sweeps;
         failed += hm[m].conv == 3;

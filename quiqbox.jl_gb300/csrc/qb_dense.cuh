@@ -7,18 +7,29 @@
 // Block-wide sum of one double per thread; every thread gets the result.  red must hold
 // 33 doubles of shared memory.
 __device__ __forceinline__ double qb_cta_sum(double v, double* red) {
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
-    __syncthreads();
+    const int tid = threadIdx.x, nw = (blockDim.x + 31) >> 5;
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+    __syncthreads();   // the previous call's readers are done with red
     if ((tid & 31) == 0) red[tid >> 5] = v;
     __syncthreads();
-    if (tid == 0) {
-        double t = 0.0;
-        for (int k = 0; k < (nt + 31) / 32; ++k) t += red[k];
-        red[32] = t;
-    }
-    __syncthreads();
-    return red[32];
+    double t = 0.0;    // every thread sums the warp totals in the same order
+    for (int k = 0; k < nw; ++k) t += red[k];
+    return t;
+}
+
+// Lanes per row for a dot product per row of `rows` rows over nt threads: the largest
+// power of two <= min(32, nt / rows) (1 when rows >= nt / 2).
+__device__ __forceinline__ int qb_group_lanes(int nt, int rows) {
+    int L = 1;
+    while (L < 32 && 2 * L * rows <= nt) L <<= 1;
+    return L;
+}
+
+// Sum over aligned groups of L lanes (L a power of two <= 32); every lane of the warp
+// must call it.
+__device__ __forceinline__ double qb_group_sum(double v, int L) {
+    for (int o = L >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
 }
 
 // C = alpha op(A) op(B) + beta C, op(A) m x k, op(B) k x n.  beta == 0 ignores C's contents.
@@ -175,6 +186,7 @@ __device__ int qb_cta_jacobi(int n, double* A, double* V, const double* Vin, dou
 template <int MAXN>
 struct QbEigSmem {
     double d[MAXN], e[MAXN], lam[MAXN], dots[MAXN];
+    float df[MAXN], e2f[MAXN];   // d and e^2 in FP32 for the Sturm counts
     double red[33];
     double bounds[3];
 };
@@ -208,15 +220,25 @@ __device__ void qb_cta_tridiag(int n, double* A, double* p, QbEigSmem<MAXN>& sm)
         for (int i = tid; i < m; i += nt) x[i] = (i == 0 ? x0 - alpha : x[i]) * inv;
         __syncthreads();
         double* S = A + (k + 1) + (size_t)n * (k + 1);
-        for (int i = tid; i < m; i += nt) {
-            double acc = 0.0;
-            for (int j = 0; j < m; ++j) acc = fma(S[i + (size_t)n * j], x[j], acc);
-            p[i] = acc;
-        }
+        // p = S x: L lanes per row (shorter dependent chains), row i's total on its first lane
+        const int L = qb_group_lanes(nt, m);
         double K = 0.0;
-        for (int i = tid; i < m; i += nt) K += x[i] * p[i];
+        for (int i0 = 0; i0 < m; i0 += nt / L) {
+            const int i = i0 + tid / L, sub = tid % L;
+            double acc = 0.0;
+            if (i < m)
+                for (int j = sub; j < m; j += L) acc = fma(S[i + (size_t)n * j], x[j], acc);
+            acc = qb_group_sum(acc, L);
+            if (i < m && sub == 0) {
+                p[i] = acc;
+                K += x[i] * acc;
+            }
+        }
         K = qb_cta_sum(K, sm.red);
-        for (int i = tid; i < m; i += nt) p[i] -= K * x[i];
+        for (int i0 = 0; i0 < m; i0 += nt / L) {
+            const int i = i0 + tid / L;
+            if (i < m && tid % L == 0) p[i] -= K * x[i];
+        }
         __syncthreads();
         for (int idx = tid; idx < m * m; idx += nt) {
             const int i = idx % m, j = idx / m;
@@ -235,69 +257,99 @@ __device__ void qb_cta_tridiag(int n, double* A, double* p, QbEigSmem<MAXN>& sm)
 }
 
 // number of eigenvalues of the tridiagonal (d, e) below x, in FP32 (pivots of the LDL^T
-// factorisation of T - x I; a pivot smaller than `tiny` is replaced by -tiny and counted
-// as negative, which keeps the count consistent when x hits a pivot exactly)
-__device__ __forceinline__ int qb_sturm_f(int n, const double* d, const double* e, float x, float tiny) {
-    float q = (float)d[0] - x;
+// factorisation of T - x I from df = d and e2f = e^2; a pivot smaller than `tiny` is
+// replaced by -tiny and counted as negative, which keeps the count consistent when x
+// hits a pivot exactly)
+__device__ __forceinline__ int qb_sturm_f(int n, const float* df, const float* e2f, float x, float tiny) {
+    float q = df[0] - x;
     if (fabsf(q) <= tiny) q = -tiny;
     int c = q < 0.f;
     for (int j = 1; j < n; ++j) {
-        const float ej = (float)e[j - 1];
-        q = (float)d[j] - x - ej * ej / q;
+        q = (df[j] - x) - __fdividef(e2f[j - 1], q);
         if (fabsf(q) <= tiny) q = -tiny;
         c += q < 0.f;
     }
     return c;
 }
 
-// z = (T - lam I)^{-1} y (T tridiagonal d, e) by Gaussian elimination with partial pivoting;
-// u0, u1, u2 (n each, strided by `ld` like y) are the rows of U.  y is overwritten by z.
-static __device__ void qb_tridiag_solve(int n, const double* d, const double* e, double lam, double pert, double* y,
-                                        double* u0, double* u1, double* u2, int ld) {
-    double m0 = d[0] - lam, m1 = n > 1 ? e[0] : 0.0, m2 = 0.0;
+// The multiplier of an LU row carries the row's swap flag in its lowest mantissa bit (a
+// one-ulp change of the multiplier).
+__device__ __forceinline__ double qb_flagged(double f, bool swap) {
+    return __longlong_as_double((__double_as_longlong(f) & ~1LL) | (swap ? 1LL : 0LL));
+}
+__device__ __forceinline__ bool qb_flag(double f) { return __double_as_longlong(f) & 1LL; }
+
+// LU of T - lam I (T tridiagonal d, e) by Gaussian elimination with partial pivoting: rows
+// j and j + 1 swap when |e_j| exceeds the pivot, a zero pivot becomes `pert`.  Per row j
+// the reciprocal pivot u0i, the superdiagonal u1 and the flagged multiplier fm; the second
+// superdiagonal of a swapped row is e_{j+1} (of an unswapped row 0).  Arrays strided by ld.
+static __device__ void qb_tridiag_factor(int n, const double* d, const double* e, double lam, double pert,
+                                         double* u0i, double* u1, double* fm, int ld) {
+    double m0 = d[0] - lam, m1 = n > 1 ? e[0] : 0.0;
     for (int j = 0; j + 1 < n; ++j) {
         const double l = e[j], a = d[j + 1] - lam, b = (j + 2 < n) ? e[j + 1] : 0.0;
-        const double rj = y[(size_t)ld * j], rn = y[(size_t)ld * (j + 1)];
         if (fabs(l) > fabs(m0)) {
             const double f = m0 / l;
-            u0[(size_t)ld * j] = l;
+            u0i[(size_t)ld * j] = 1.0 / l;
             u1[(size_t)ld * j] = a;
-            u2[(size_t)ld * j] = b;
-            y[(size_t)ld * j] = rn;
-            y[(size_t)ld * (j + 1)] = rj - f * rn;
+            fm[(size_t)ld * j] = qb_flagged(f, true);
             m0 = m1 - f * a;
-            m1 = m2 - f * b;
-            m2 = 0.0;
+            m1 = -f * b;
         } else {
             if (m0 == 0.0) m0 = pert;
             const double f = l / m0;
-            u0[(size_t)ld * j] = m0;
+            u0i[(size_t)ld * j] = 1.0 / m0;
             u1[(size_t)ld * j] = m1;
-            u2[(size_t)ld * j] = m2;
-            y[(size_t)ld * (j + 1)] = rn - f * rj;
+            fm[(size_t)ld * j] = qb_flagged(f, false);
             m0 = a - f * m1;
-            m1 = b - f * m2;
-            m2 = 0.0;
+            m1 = b;
         }
     }
     if (m0 == 0.0) m0 = pert;
-    u0[(size_t)ld * (n - 1)] = m0;
+    u0i[(size_t)ld * (n - 1)] = 1.0 / m0;
+    u1[(size_t)ld * (n - 1)] = 0.0;
+    fm[(size_t)ld * (n - 1)] = 0.0;
+}
+
+// y <- (T - lam I)^{-1} y with the factors of qb_tridiag_factor (same stride ld).
+static __device__ void qb_tridiag_apply(int n, const double* e, const double* u0i, const double* u1,
+                                        const double* fm, double* y, int ld) {
+    double cur = y[0];
+    for (int j = 0; j + 1 < n; ++j) {
+        const double f = fm[(size_t)ld * j], nxt = y[(size_t)ld * (j + 1)];
+        const bool sw = qb_flag(f);
+        const double a = sw ? nxt : cur, b = sw ? cur : nxt;
+        y[(size_t)ld * j] = a;
+        cur = b - f * a;
+    }
+    y[(size_t)ld * (n - 1)] = cur;
+    double z1 = 0.0, z2 = 0.0;   // z_{j+1}, z_{j+2}
     for (int j = n - 1; j >= 0; --j) {
-        double s = y[(size_t)ld * j];
-        if (j + 1 < n) s -= u1[(size_t)ld * j] * y[(size_t)ld * (j + 1)];
-        if (j + 2 < n) s -= u2[(size_t)ld * j] * y[(size_t)ld * (j + 2)];
-        y[(size_t)ld * j] = s / u0[(size_t)ld * j];
+        double s = y[(size_t)ld * j] - u1[(size_t)ld * j] * z1;
+        if (j + 2 < n && qb_flag(fm[(size_t)ld * j])) s -= e[j + 1] * z2;
+        const double z = s * u0i[(size_t)ld * j];
+        y[(size_t)ld * j] = z;
+        z2 = z1;
+        z1 = z;
     }
 }
 
 // k lowest eigenpairs of the symmetric n x n matrix A (destroyed): eigenvalues in w[0..k),
 // eigenvectors in the columns of Y (n x k, column-major).  B0, B1, B2 are n x k scratch
-// (band rows of the inverse-iteration LU) and p n doubles of scratch.
+// and p n doubles of scratch.  Eigenvalue i (and its vector) belongs to lane i / 4 of warp
+// i % 4, which spreads the serial per-eigenvalue work over the four SM sub-partitions;
+// the inverse-iteration vectors and LU factors are interleaved (entry j of vector i at
+// j k + i) so that a warp's lanes read neighbouring addresses.
 template <int MAXN>
 __device__ void qb_cta_lowest_eig(int n, int k, double* A, double* Y, double* w, double* B0, double* B1, double* B2,
                                   double* p, QbEigSmem<MAXN>& sm) {
     const int tid = threadIdx.x, nt = blockDim.x;
     qb_cta_tridiag<MAXN>(n, A, p, sm);
+    for (int j = tid; j < n; j += nt) {
+        sm.df[j] = (float)sm.d[j];
+        const float ef = j + 1 < n ? (float)sm.e[j] : 0.0f;
+        sm.e2f[j] = ef * ef;
+    }
     if (tid == 0) {   // Gershgorin interval and the scale of T
         double lo = 0.0, hi = 0.0;
         for (int i = 0; i < n; ++i) {
@@ -313,48 +365,75 @@ __device__ void qb_cta_lowest_eig(int n, int k, double* A, double* Y, double* w,
     __syncthreads();
     const double nrm = sm.bounds[2];
     const double pert = 1e-16 * nrm;
-    // eigenvalue i by FP32 bisection, refined by FP64 Rayleigh-quotient inverse iteration
-    for (int i = tid; i < k; i += nt) {
+    // eigenvalue i by a group of G lanes: FP32 multisection on Sturm counts (each round
+    // splits the bracket into G + 1 parts), then the group's first lane runs the inverse
+    // iteration for eigenvector i
+    const int G = min(8, qb_group_lanes(nt, k));
+    const int ngrp = nt / G, lane = tid & 31, sub = tid % G;
+    const float tiny = (float)(1e-30 * nrm) + 1e-30f;
+    const float absres = (float)(1e-13 * nrm);
+    double* Yt = B0;   // interleaved vectors; B1, B2 and Y hold the interleaved LU factors
+    for (int i0 = 0; i0 < k; i0 += ngrp) {
+        const int i = i0 + tid / G;
         float lo = (float)sm.bounds[0], hi = (float)sm.bounds[1];
-        const float tiny = (float)(1e-30 * nrm) + 1e-30f;
-        for (int it = 0; it < 64; ++it) {
-            const float mid = 0.5f * (lo + hi);
-            if (!(mid > lo && mid < hi)) break;
-            if (qb_sturm_f(n, sm.d, sm.e, mid, tiny) > i) hi = mid;
-            else lo = mid;
+        bool frozen = i >= k;
+        for (int round = 0; round < 64; ++round) {
+            if (__all_sync(0xffffffffu, frozen)) break;
+            const float step = (hi - lo) / (float)(G + 1);
+            const float x = fminf(lo + step * (float)(sub + 1), hi);
+            const bool above = !frozen && qb_sturm_f(n, sm.df, sm.e2f, x, tiny) > i;
+            const unsigned gm = (__ballot_sync(0xffffffffu, above) >> (lane & ~(G - 1))) & ((1u << G) - 1u);
+            if (!frozen) {
+                const int s = gm ? __ffs(gm) - 1 : G;   // first point above eigenvalue i
+                const float nlo = s > 0 ? fminf(lo + step * (float)s, hi) : lo;
+                const float nhi = s < G ? fminf(lo + step * (float)(s + 1), hi) : hi;
+                lo = nlo;
+                hi = nhi;
+                frozen = !(hi - lo > 2.4e-7f * fmaxf(fabsf(lo), fabsf(hi)) + absres);
+            }
         }
-        const double lam = 0.5 * ((double)lo + (double)hi);
-        double* y = Y + (size_t)n * i;
-        for (int j = 0; j < n; ++j) {   // deterministic start vector, distinct per eigenvalue
-            const unsigned h = (unsigned)(j * 2654435761u) ^ (unsigned)(i * 40503u + 17u);
-            y[j] = 1.0 + 0.25 * ((double)(h & 0xffff) / 65536.0 - 0.5);
+        if (i < k && sub == 0) {
+            const double lam = 0.5 * ((double)lo + (double)hi);
+            double* y = Yt + i;
+            for (int j = 0; j < n; ++j) {   // deterministic start vector, distinct per eigenvalue
+                const unsigned h = (unsigned)(j * 2654435761u) ^ (unsigned)(i * 40503u + 17u);
+                y[(size_t)k * j] = 1.0 + 0.25 * ((double)(h & 0xffff) / 65536.0 - 0.5);
+            }
+            // inverse iteration at the fixed FP32 shift (within ~1e-7 ||T|| of the eigenvalue):
+            // components of eigenvalues further than 1e-4 ||T|| shrink by >= 1e3 per step
+            qb_tridiag_factor(n, sm.d, sm.e, lam, pert, B1 + i, B2 + i, Y + i, k);
+            for (int s = 0; s < 6; ++s) {
+                qb_tridiag_apply(n, sm.e, B1 + i, B2 + i, Y + i, y, k);
+                double nn2 = 0.0;
+                for (int j = 0; j < n; ++j) nn2 = fma(y[(size_t)k * j], y[(size_t)k * j], nn2);
+                const double inv = 1.0 / sqrt(nn2);
+                for (int j = 0; j < n; ++j) y[(size_t)k * j] *= inv;
+            }
+            sm.lam[i] = lam;
         }
-        // inverse iteration at the fixed FP32 shift (within ~1e-7 ||T|| of the eigenvalue):
-        // components of eigenvalues further than 1e-4 ||T|| shrink by >= 1e3 per step
-        for (int s = 0; s < 6; ++s) {
-            qb_tridiag_solve(n, sm.d, sm.e, lam, pert, y, B0 + (size_t)n * i, B1 + (size_t)n * i,
-                             B2 + (size_t)n * i, 1);
-            double nn2 = 0.0;
-            for (int j = 0; j < n; ++j) nn2 += y[j] * y[j];
-            const double inv = 1.0 / sqrt(nn2);
-            for (int j = 0; j < n; ++j) y[j] *= inv;
-        }
-        sm.lam[i] = lam;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < n * k; idx += nt) {   // Y (column-major) <- the interleaved vectors
+        const int j = idx % n, i = idx / n;
+        Y[idx] = Yt[(size_t)k * j + i];
     }
     __syncthreads();
     // Gram-Schmidt within clusters (|lam_i - lam_j| <= 1e-4 ||T||: the eigenvalues inverse
     // iteration cannot separate), normalisation
-    for (int i = 0; i < k; ++i) {
+    for (int i = 1; i < k; ++i) {
+        // vectors without a close predecessor are already normalised and need nothing
+        if (sm.lam[i] - sm.lam[i - 1] > 1e-4 * nrm) continue;
         double* yi = Y + (size_t)n * i;
-        for (int j = 0; j < i; ++j) {
-            if (fabs(sm.lam[i] - sm.lam[j]) > 1e-4 * nrm) continue;
-            const double* yj = Y + (size_t)n * j;
-            double dot = 0.0;
-            for (int r = tid; r < n; r += nt) dot += yi[r] * yj[r];
-            dot = qb_cta_sum(dot, sm.red);
-            for (int r = tid; r < n; r += nt) yi[r] -= dot * yj[r];
-            __syncthreads();
-        }
+        for (int pass = 0; pass < 2; ++pass)   // twice: vectors of one cluster can be nearly parallel
+            for (int j = 0; j < i; ++j) {
+                if (fabs(sm.lam[i] - sm.lam[j]) > 1e-4 * nrm) continue;
+                const double* yj = Y + (size_t)n * j;
+                double dot = 0.0;
+                for (int r = tid; r < n; r += nt) dot += yi[r] * yj[r];
+                dot = qb_cta_sum(dot, sm.red);
+                for (int r = tid; r < n; r += nt) yi[r] -= dot * yj[r];
+                __syncthreads();
+            }
         double nn2 = 0.0;
         for (int r = tid; r < n; r += nt) nn2 += yi[r] * yi[r];
         nn2 = qb_cta_sum(nn2, sm.red);
@@ -375,14 +454,19 @@ __device__ void qb_cta_lowest_eig(int n, int k, double* A, double* Y, double* w,
     }
     __syncthreads();
     // back-transformation: Y <- H_0 H_1 ... H_{n-3} Y
+    const int LB = qb_group_lanes(nt, k);
     for (int kk = n - 3; kk >= 0; --kk) {
         const int m = n - kk - 1;
         const double* v = A + (kk + 1) + (size_t)n * kk;
-        for (int c = tid; c < k; c += nt) {
-            const double* yc = Y + (size_t)n * c + kk + 1;
+        for (int c0 = 0; c0 < k; c0 += nt / LB) {   // LB lanes per column
+            const int c = c0 + tid / LB, sb = tid % LB;
             double dot = 0.0;
-            for (int r = 0; r < m; ++r) dot = fma(v[r], yc[r], dot);
-            sm.dots[c] = dot;
+            if (c < k) {
+                const double* yc = Y + (size_t)n * c + kk + 1;
+                for (int r = sb; r < m; r += LB) dot = fma(v[r], yc[r], dot);
+            }
+            dot = qb_group_sum(dot, LB);
+            if (c < k && sb == 0) sm.dots[c] = dot;
         }
         __syncthreads();
         for (int idx = tid; idx < m * k; idx += nt) {

@@ -33,6 +33,7 @@ NIN, NHID, NLAYER, NOUT = 128, 256, 4, 64
 NFEAT = 74
 MU = 0.25 + 0.25 * np.arange(32)
 WEIGHTS_FILE = Path(__file__).resolve().parent / "data" / "guess_mlp.npz"
+FALLBACK_ITER = 60      # learned-guess iterations before the core-Hamiltonian restart
 
 
 # ---------------------------------------------------------------------------
@@ -49,89 +50,77 @@ def atom_offsets(symbols):
     return off, o
 
 
-def _unit(v):
-    return v / np.maximum(np.linalg.norm(v, axis=-1, keepdims=True), 1e-300)
-
-
-def pair_data(mols):
-    """Pairs (a <= b) of every molecule with their local frames and features.
-
-    Local frame: for a != b, z along A -> B and x towards the atom nearest the bond
-    midpoint (its component perpendicular to z); for a == b, z towards the nearest
-    neighbour and x towards the second nearest.  Without such an atom x is any unit
-    vector perpendicular to z.  Features (74 used of NIN): 32 Gaussian-expanded r_AB, a
-    same-atom flag, element one-hots of A and B, per endpoint and per element of the
-    neighbours sum w (1, cos_z, cos_x, (3 cos_z^2 - 1) / 2) with w = exp(-(r / 2.5)^2)
-    in the local frame, and the molecular charge."""
-    nats = np.array([len(m["symbols"]) for m in mols])
-    nat = int(nats.max())
-    nm = len(mols)
-    pos = np.zeros((nm, nat, 3))
-    el = np.full((nm, nat), -1, np.int64)
+def pair_index(mols):
+    """Host-side index arrays of every atom pair (a <= b) of every molecule: molecule and
+    local / global atom indices, atoms' positions, elements and first functions, the
+    molecules' sizes and offsets of their column-major densities (vectorised numpy)."""
     code = {e: i for i, e in enumerate(ELEMENTS)}
-    for k, m in enumerate(mols):
-        na = nats[k]
-        pos[k, :na] = m["coords"]
-        el[k, :na] = [code[x] for x in m["symbols"]]
+    nats = np.array([len(m["symbols"]) for m in mols], np.int64)
+    nm = len(mols)
+    atom0 = np.zeros(nm, np.int64)
+    atom0[1:] = np.cumsum(nats)[:-1]
+    pos = np.concatenate([np.asarray(m["coords"], np.float64).reshape(-1, 3) for m in mols])
+    el = np.array([code[s] for m in mols for s in m["symbols"]], np.int32)
     tri = {n: np.triu_indices(n) for n in np.unique(nats)}
     cnt = nats * (nats + 1) // 2
     pm = np.repeat(np.arange(nm), cnt)
-    pa = np.concatenate([tri[n][0] for n in nats])
-    pb = np.concatenate([tri[n][1] for n in nats])
-    npair = len(pm)
-    PA, PB = pos[pm, pa], pos[pm, pb]
-    same = pa == pb
-    neigh = pos[pm]                                   # (npair, nat, 3)
-    nel = el[pm]                                      # (npair, nat)
-    valid = nel >= 0
-    idx = np.arange(nat)[None, :]
-    dA = np.linalg.norm(neigh - PA[:, None, :], axis=2)
-    # z axis
-    z = _unit(PB - PA)
-    dA_other = np.where(valid & (idx != pa[:, None]), dA, np.inf)
-    order = np.argsort(dA_other, axis=1)
-    n1 = order[:, 0]
-    z_same = _unit(neigh[np.arange(npair), n1] - PA)
-    has1 = np.isfinite(dA_other[np.arange(npair), n1])
-    z = np.where(same[:, None], np.where(has1[:, None], z_same, np.array([0.0, 0.0, 1.0])), z)
-    # x axis: reference atom (midpoint-nearest third atom, or second-nearest neighbour)
-    mid = 0.5 * (PA + PB)
-    dmid = np.linalg.norm(neigh - mid[:, None, :], axis=2)
-    excl = (idx == pa[:, None]) | (idx == pb[:, None])
-    rel = neigh - PA[:, None, :]
-    perp = rel - np.sum(rel * z[:, None, :], axis=2, keepdims=True) * z[:, None, :]
-    pn = np.linalg.norm(perp, axis=2)
-    cand_pair = np.where(valid & ~excl & (pn > 0.3), dmid, np.inf)
-    cand_same = np.where(valid & (idx != pa[:, None]) & (idx != n1[:, None]) & (pn > 0.3), dA, np.inf)
-    cand = np.where(same[:, None], cand_same, cand_pair)
-    ref_i = np.argmin(cand, axis=1)
-    has_ref = np.isfinite(cand[np.arange(npair), ref_i])
-    xr = perp[np.arange(npair), ref_i]
-    helper = np.where(np.abs(z[:, 2:3]) < 0.9, np.array([0.0, 0.0, 1.0]), np.array([1.0, 0.0, 0.0]))
-    xa = np.cross(helper, z)
-    x = _unit(np.where(has_ref[:, None], xr, xa))
-    y = np.cross(z, x)
-    R = np.stack([x, y, z], axis=2)                  # columns: local axes in lab coordinates
-    # features
-    X = np.zeros((npair, NIN), np.float32)
-    r = np.linalg.norm(PB - PA, axis=1)
-    X[:, :32] = np.exp(-((r[:, None] - MU[None, :]) / 0.25) ** 2)
-    X[:, 32] = same
-    X[np.arange(npair), 33 + el[pm, pa]] = 1.0
-    X[np.arange(npair), 37 + el[pm, pb]] = 1.0
-    for e_off, (P, me) in enumerate(((PA, pa), (PB, pb))):
-        u = neigh - P[:, None, :]
-        d = np.linalg.norm(u, axis=2)
-        w = np.where(valid & (idx != me[:, None]), np.exp(-(d / 2.5) ** 2), 0.0)
-        dn = np.maximum(d, 1e-12)
-        cz = np.sum(u * z[:, None, :], axis=2) / dn
-        cx = np.sum(u * x[:, None, :], axis=2) / dn
-        terms = np.stack([w, w * cz, w * cx, w * 0.5 * (3 * cz * cz - 1)], axis=2)   # (npair, nat, 4)
-        for e in range(4):
-            sel = (nel == e)[:, :, None]
-            X[:, 41 + 16 * e_off + 4 * e:41 + 16 * e_off + 4 * e + 4] = np.sum(terms * sel, axis=1)
-    X[:, 73] = np.array([m["charge"] for m in mols], np.float32)[pm]
-    return {"mol": pm, "a": pa, "b": pb, "R": R, "X": X}
+    pa = np.concatenate([tri[n][0] for n in nats]).astype(np.int64)
+    pb = np.concatenate([tri[n][1] for n in nats]).astype(np.int64)
+    nb = np.where(el == 0, 1, 5)
+    fx = np.cumsum(nb) - nb                              # global first function of each atom
+    atom_f0 = (fx - np.repeat(fx[atom0], nats)).astype(np.int32)
+    mol_n = np.add.reduceat(nb, atom0).astype(np.int32)
+    mol_off = np.zeros(nm, np.int64)
+    mol_off[1:] = np.cumsum(mol_n.astype(np.int64) ** 2)[:-1]
+    return {"mol": pm, "a": pa, "b": pb, "ga": atom0[pm] + pa, "gb": atom0[pm] + pb, "atom0": atom0, "nats": nats,
+            "pos": pos, "el": el, "atom_f0": atom_f0, "mol_n": mol_n, "mol_off": mol_off,
+            "charge": np.array([m["charge"] for m in mols], np.float32)}
+
+
+def pair_data(mols, lib, device="cuda:0", host=True):
+    """Pairs of every molecule with their local frames and network inputs, computed on the
+    device by qb_guess_features (csrc/guess.cu describes the frames and features).
+    Returns the index arrays of pair_index plus device tensors "Xd" (rows padded to a
+    multiple of 64, zero beyond the pairs) and "Rd"; with host=True also "X" (npair x 128)
+    and "R" (npair x 3 x 3, columns the local axes) as numpy arrays."""
+    import torch
+    pd = pair_index(mols)
+    dev = torch.device(device)
+    npair = len(pd["mol"])
+    M = max(64, ((npair + 63) // 64) * 64)
+    t = {k: torch.tensor(pd[k], dtype=torch.int32, device=dev) for k in ("mol", "ga", "gb", "atom0", "nats", "el",
+                                                                          "atom_f0", "mol_n")}
+    t["pos"] = torch.tensor(pd["pos"], device=dev)
+    t["charge"] = torch.tensor(pd["charge"], device=dev)
+    t["mol_off"] = torch.tensor(pd["mol_off"], device=dev)
+    Xd = torch.zeros((M, NIN), dtype=torch.float32, device=dev)
+    Rd = torch.empty((max(npair, 1), 9), dtype=torch.float64, device=dev)
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    rc = lib.qb_guess_features(npair, _ptr(t["mol"]), _ptr(t["ga"]), _ptr(t["gb"]), _ptr(t["atom0"]),
+                               _ptr(t["nats"]), _ptr(t["pos"]), _ptr(t["el"]), _ptr(t["charge"]), _ptr(Xd),
+                               _ptr(Rd), stream)
+    if rc != 0:
+        raise RuntimeError(f"qb_guess_features failed with status {rc}")
+    pd.update({"Xd": Xd, "Rd": Rd, "dev": t, "stream": stream, "npair": npair})
+    if host:
+        pd["X"] = Xd[:npair].cpu().numpy()
+        pd["R"] = Rd[:npair].cpu().numpy().reshape(npair, 3, 3)
+    return pd
+
+
+def assemble_device(lib, pd, Yd):
+    """Per-spin initial densities of all molecules (device, column-major, concatenated)
+    from the network's output rows Yd (device, one row per pair) by qb_guess_assemble."""
+    import torch
+    t = pd["dev"]
+    total = int(pd["mol_off"][-1] + int(pd["mol_n"][-1]) ** 2) if len(pd["mol_n"]) else 0
+    D = torch.zeros(max(total, 1), dtype=torch.float64, device=Yd.device)
+    rc = lib.qb_guess_assemble(pd["npair"], _ptr(t["mol"]), _ptr(t["ga"]), _ptr(t["gb"]), _ptr(t["el"]),
+                               _ptr(t["atom_f0"]), _ptr(t["mol_off"]), _ptr(t["mol_n"]), _ptr(Yd), Yd.shape[1],
+                               _ptr(pd["Rd"]), _ptr(D), pd["stream"])
+    if rc != 0:
+        raise RuntimeError(f"qb_guess_assemble failed with status {rc}")
+    return D
 
 
 def _gather_index(symbols):
@@ -170,27 +159,6 @@ def blocks_from_densities(mols, dens, pd):
         Wm[sl, :25] = mask.reshape(cnt, 25)
         start += cnt
     return Y, Wm
-
-
-def densities_from_blocks(mols, pd, Ypred):
-    T = _T5(pd["R"])
-    out, start = [], 0
-    for m in mols:
-        gi, n = _gather_index(m["symbols"])
-        cnt = len(m["symbols"]) * (len(m["symbols"]) + 1) // 2
-        sl = slice(start, start + cnt)
-        loc = np.asarray(Ypred[sl, :25], float).reshape(cnt, 5, 5)
-        blk = np.einsum("pij,pjk,plk->pil", T[sl], loc, T[sl])
-        a, b = pd["a"][sl], pd["b"][sl]
-        diag = a == b
-        blk[diag] = 0.5 * (blk[diag] + np.transpose(blk[diag], (0, 2, 1)))
-        Dp = np.zeros((n + 1, n + 1))
-        ia, ib = gi[a], gi[b]
-        Dp[ib[:, :, None], ia[:, None, :]] = np.transpose(blk, (0, 2, 1))
-        Dp[ia[:, :, None], ib[:, None, :]] = blk
-        out.append(Dp[:n, :n].copy())
-        start += cnt
-    return out
 
 
 # ---------------------------------------------------------------------------
@@ -336,6 +304,11 @@ class GuessMLP:
         Y, _ = self.forward(self.to_bf16(x))
         return Y[:n].cpu().numpy()
 
+    def predict_device(self, Xd):
+        """Xd (M, NIN) float32 on the device, M a multiple of 64 -> Y (M, NOUT) on the device."""
+        Y, _ = self.forward(self.to_bf16(Xd))
+        return Y
+
 
 def _pad_rows(a, mult=64):
     n = a.shape[0]
@@ -348,8 +321,10 @@ def _pad_rows(a, mult=64):
 
 
 # ---------------------------------------------------------------------------
-def dataset(mols, densities):
-    pd = pair_data(mols)
+def dataset(mols, densities, lib=None):
+    """Network inputs (device features) and local-frame target blocks with their masks."""
+    from . import _lib as L
+    pd = pair_data(mols, lib or L.load())
     Y, W = blocks_from_densities(mols, densities, pd)
     return pd["X"], Y, W
 
@@ -387,10 +362,23 @@ def load(lib, device="cuda:0", path=WEIGHTS_FILE):
     return GuessMLP(lib, device, params={k: p[k] for k in p.files if k[0] in "Wb"})
 
 
+def initial_density_device(net, mols):
+    """Learned initial per-spin densities of generated molecules, all on the device:
+    features, network and assembly; returns the concatenated column-major densities (the
+    batched SCF's initial-density layout) as one float64 device tensor."""
+    pd = pair_data(mols, net.lib, device=net.dev, host=False)
+    return assemble_device(net.lib, pd, net.predict_device(pd["Xd"]))
+
+
 def initial_densities(net, mols):
-    """Learned initial per-spin densities of a list of generated molecules."""
-    pd = pair_data(mols)
-    return densities_from_blocks(mols, pd, net.predict(pd["X"]))
+    """Learned initial per-spin densities as a list of host matrices."""
+    D = initial_density_device(net, mols).cpu().numpy()
+    out, off = [], 0
+    for m in mols:
+        n = m["flat"].nfun
+        out.append(D[off:off + n * n].reshape((n, n), order="F"))
+        off += n * n
+    return out
 
 
 def train_main(n_train=20000, n_test=2000, seed_train=101, seed_test=202, epochs=20, out=WEIGHTS_FILE,
@@ -431,44 +419,50 @@ def train_main(n_train=20000, n_test=2000, seed_train=101, seed_test=202, epochs
     return info
 
 
-def solve_with_guess(qb, net, mols, fallback=True, first_max_iter=100):
-    """Batched SCF from the learned guess; molecules it has not converged after
-    `first_max_iter` iterations are solved again from the core-Hamiltonian guess (the
-    fallback).  Returns (result, fallback indices)."""
+def solve_with_guess(qb, net, mols, fallback_iter=FALLBACK_ITER, max_iter=200):
+    """Batched SCF from the learned guess in one call; a molecule the learned density has
+    not converged after `fallback_iter` iterations restarts from the core-Hamiltonian
+    guess inside the same call (0: no fallback), all iterations counted against
+    `max_iter`.  Returns (result, indices of the restarted molecules)."""
     args = [(m["nuc"], m["flat"], m["charge"]) for m in mols]
-    D0 = initial_densities(net, mols)
-    cfg = qb.BatchSCFConfig(max_iter=first_max_iter if fallback else 200)
+    D0 = initial_density_device(net, mols)
+    cfg = qb.BatchSCFConfig(max_iter=max_iter, fallback_iter=fallback_iter)
     res = qb.runHartreeFockBatched(args, config=cfg, initial_densities=D0)
-    redo = [k for k in range(len(mols)) if not res.converged[k]] if fallback else []
-    if redo:
-        r2 = qb.runHartreeFockBatched([args[k] for k in redo])
-        for j, k in enumerate(redo):
-            res.energies[k] = r2.energies[j]
-            res.elec_energies[k] = r2.elec_energies[j]
-            res.iterations[k] += r2.iterations[j]
-            res.converged[k] = r2.converged[j]
-    return res, redo
+    return res, [int(k) for k in np.nonzero(res.restarted)[0]]
 
 
-def evaluate(qb, net, n_test=2000, seed=202):
+def evaluate(qb, net, n_test=2000, seed=202, fallback_iter=FALLBACK_ITER):
+    """Held-out comparison of the core-Hamiltonian and learned guesses (both one batched
+    call, at most 200 iterations per molecule)."""
+    import torch
     from quiqbox_gb300.workloads import batch_molecules
     mols = batch_molecules(n_test, seed=seed, atoms=(3, 12), basis_names=("STO-3G",))
     args = [(m["nuc"], m["flat"], m["charge"]) for m in mols]
-    qb.runHartreeFockBatched(args[:16])   # warm-up
+    qb.runHartreeFockBatched(args[:16])   # warm-up of both paths
+    solve_with_guess(qb, net, mols[:16], fallback_iter)
     t0 = time.perf_counter()
     base = qb.runHartreeFockBatched(args)
     t_base = time.perf_counter() - t0
     t0 = time.perf_counter()
-    lrn, redo = solve_with_guess(qb, net, mols)
+    lrn, redo = solve_with_guess(qb, net, mols, fallback_iter)
     t_lrn = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    initial_density_device(net, mols)
+    torch.cuda.synchronize()
+    t_guess = time.perf_counter() - t0
     both = base.converged & lrn.converged
     dE = np.abs(base.energies[both] - lrn.energies[both])
     return {"molecules": n_test, "coreh_converged": int(base.converged.sum()),
-            "learned_converged": int(lrn.converged.sum()), "fallback": len(redo),
+            "learned_converged": int(lrn.converged.sum()), "fallback_iter": fallback_iter,
+            "restarted_from_coreh": len(redo),
             "coreh_mean_iterations": float(base.iterations[both].mean()),
             "learned_mean_iterations": float(lrn.iterations[both].mean()),
-            "coreh_wall_s": t_base, "learned_wall_s": t_lrn,
+            "coreh_median_iterations": float(np.median(base.iterations[both])),
+            "learned_median_iterations": float(np.median(lrn.iterations[both])),
+            "coreh_wall_s": t_base, "learned_wall_s": t_lrn, "learned_guess_s": t_guess,
+            "coreh_ms_scf": base.ms_scf, "learned_ms_scf": lrn.ms_scf,
             "coreh_solves_per_s": float(base.converged.sum() / t_base),
             "learned_solves_per_s": float(lrn.converged.sum() / t_lrn),
-            "max_abs_dE_same_state": float(np.sort(dE)[int(0.99 * len(dE))]) if len(dE) else None,
+            "p99_abs_dE_both_converged": float(np.sort(dE)[int(0.99 * (len(dE) - 1))]) if len(dE) else None,
             "frac_same_state_1e-8": float((dE < 1e-8).mean()) if len(dE) else None}

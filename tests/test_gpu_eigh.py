@@ -51,3 +51,16 @@ def test_degenerate_and_h2_like(qb):
         A = B + B.T
         np.fill_diagonal(A, 1.0)
         _check(qb, A, max(1, n // 2))
+    # block-diagonal copies of one block: every eigenvalue threefold, clusters across the
+    # occupied/virtual boundary handled by the subspace test only
+    B = rng.normal(size=(7, 7))
+    blk = B + B.T
+    A = np.kron(np.eye(3), blk)
+    _check(qb, A, 9)
+    # near-degenerate pairs (split 1e-7, inside the Gram-Schmidt cluster tolerance) and a
+    # large diagonal shift
+    Q = np.linalg.qr(rng.normal(size=(24, 24)))[0]
+    w = np.repeat(np.sort(rng.normal(size=12)), 2)
+    w[1::2] += 1e-7
+    _check(qb, Q @ np.diag(w) @ Q.T, 12, tol=1e-9)
+    _check(qb, 1e4 * np.eye(30) + (lambda M: M + M.T)(rng.normal(size=(30, 30))), 12, tol=1e-10)

