@@ -52,6 +52,9 @@ def parse():
                     help="held-out molecules of the learned-guess measurement (0 skips it)")
     ap.add_argument("--jk-only", type=int, default=0,
                     help="profiling driver: prepare the workload, run this many J/K builds, print timings, exit")
+    ap.add_argument("--batched-only", type=int, default=0,
+                    help="profiling driver: one batched RHF call over this many molecules of the learned-guess "
+                         "test set (3-12 atoms, STO-3G, core-Hamiltonian guess), print timings, exit")
     return ap.parse_args()
 
 
@@ -542,10 +545,28 @@ def run_jk_only(args):
     print(json.dumps({"class_quartets_prim_quartets": classes}), flush=True)
 
 
+def run_batched_only(args):
+    """One batched RHF call (after a small warm-up call) for launch-list captures."""
+    import __graft_entry__ as ge
+    qb = ge.load_package()
+    from quiqbox_gb300.workloads import batch_molecules
+    mols = batch_molecules(args.batched_only, seed=202, atoms=(3, 12), basis_names=("STO-3G",))
+    mol_args = [(m["nuc"], m["flat"], m["charge"]) for m in mols]
+    qb.runHartreeFockBatched(mol_args[:4], config=qb.BatchSCFConfig(max_iter=4))
+    t0 = time.perf_counter()
+    r = qb.runHartreeFockBatched(mol_args)
+    print(json.dumps({"wall_s": time.perf_counter() - t0, "ms_integrals": r.ms_integrals, "ms_scf": r.ms_scf,
+                      "converged": int(r.converged.sum()), "quartets": int(r.quartets),
+                      "prim_quartets": int(r.prim_quartets), "graph_launches": int(r.graph_launches)}), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.jk_only:
         run_jk_only(a)
+        sys.exit(0)
+    if a.batched_only:
+        run_batched_only(a)
         sys.exit(0)
     if a.warmup < 3:
         a.warmup = 3

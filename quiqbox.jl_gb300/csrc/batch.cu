@@ -139,34 +139,6 @@ __global__ void __launch_bounds__(128) qb_batch_digest_kernel(const BatchWork w,
     }
 }
 
-// Schwarz factors Q_ab = max over components sqrt|(ab|ab)| of one pair class, from the
-// class's own primitive-pair quartet code (the shell integrals times the per-function
-// ratios r_a r_b of the basis weights).
-template <int LA, int LB>
-__global__ void __launch_bounds__(128) qb_batch_schwarz_kernel(const ShellPair* __restrict__ pairs, int n,
-                                                               const PrimPair* __restrict__ prims,
-                                                               const double* __restrict__ boys,
-                                                               const double* __restrict__ ratio,
-                                                               double* __restrict__ Q) {
-    using C = EriClass<LA, LB, LA, LB>;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const ShellPair P = pairs[k];
-    double I[C::NINT];
-    unsigned cnt = 0;
-    C::block(prims + P.prim0, P.nprim, prims + P.prim0, P.nprim, P.ABx, P.ABy, P.ABz, P.ABx, P.ABy, P.ABz, boys, I,
-             cnt);
-    double mx = 0.0;
-#pragma unroll
-    for (int x = 0; x < C::NA; ++x)
-#pragma unroll
-        for (int y = 0; y < C::NB; ++y) {
-            const double r = __ldg(ratio + P.fa + x) * __ldg(ratio + P.fb + y);
-            mx = fmax(mx, fabs(I[((x * C::NB + y) * C::NA + x) * C::NB + y]) * r * r);
-        }
-    Q[k] = sqrt(mx);
-}
-
 // X = S^{-1/2} by the eigen-decomposition of S; C' = I; D = D' = 0, or with an initial
 // density D0 (already in D): D' = S^{1/2} D0 S^{1/2}, D~ = ratio-scaled D0, and the SCF
 // starts at iteration 1 (the first step builds F from D0).
@@ -710,9 +682,9 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
         const ShellPair* pp = d_pairs.p + pc_off[pc];
         double* q = d_Q.p + pc_off[pc];
         const int g = (n + 127) / 128;
-        if (pc == 0) qb_batch_schwarz_kernel<0, 0><<<g, 128, 0, s>>>(pp, n, d_prims.p, ctx->boys.p, d_ratio.p, q);
-        else if (pc == 1) qb_batch_schwarz_kernel<1, 0><<<g, 128, 0, s>>>(pp, n, d_prims.p, ctx->boys.p, d_ratio.p, q);
-        else qb_batch_schwarz_kernel<1, 1><<<g, 128, 0, s>>>(pp, n, d_prims.p, ctx->boys.p, d_ratio.p, q);
+        if (pc == 0) qb_schwarz_class_kernel<0, 0><<<g, 128, 0, s>>>(pp, n, d_prims.p, ctx->boys.p, d_ratio.p, q);
+        else if (pc == 1) qb_schwarz_class_kernel<1, 0><<<g, 128, 0, s>>>(pp, n, d_prims.p, ctx->boys.p, d_ratio.p, q);
+        else qb_schwarz_class_kernel<1, 1><<<g, 128, 0, s>>>(pp, n, d_prims.p, ctx->boys.p, d_ratio.p, q);
         QB_CUDA(ctx, cudaGetLastError());
     }
     QB_TRY(qb_check_status(ctx));

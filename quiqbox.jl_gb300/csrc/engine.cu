@@ -358,15 +358,22 @@ int qb_ensure_pairs(qb_ctx* ctx) {
         for (int k = 0; k < npair; ++k) pairs[k].nprim = nkept[k];
         QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_pairs.p, pairs.data(), npair * sizeof(ShellPair), cudaMemcpyHostToDevice, s));
     }
-    // Schwarz factors (generic kernel over the diagonal function quartets of every pair)
+    // Schwarz factors from the diagonal classes' own quartet code
     for (int pc = 0; pc < npc; ++pc) {
         int la = 0;
         while ((la + 1) * (la + 2) / 2 <= pc) ++la;
         const int lb = pc - la * (la + 1) / 2;
         const int n = ctx->pc_off[pc + 1] - ctx->pc_off[pc];
-        if (qb_gen_schwarz(qb_gen_basis(ctx), ctx->boys.p, ctx->d_pairs.p + ctx->pc_off[pc], n, (la + 1) * (la + 2) / 2,
-                           (lb + 1) * (lb + 2) / 2, ctx->d_Q.p + ctx->pc_off[pc], ctx->status.p, s) != 0)
-            return qb_cuda_check(ctx, cudaGetLastError(), "Schwarz kernel");
+        if (n == 0) continue;
+        QbSchwarzLaunch launch = nullptr;
+        for (int c = 0; c < QB_NCLASS; ++c) {
+            const ClassLaunchers& L = ctx->launch[c];
+            if (L.la == la && L.lb == lb && L.lc == la && L.ld == lb) launch = L.schwarz;
+        }
+        if (!launch) return qb_set_error(ctx, QB_ERR_UNSUPPORTED, "no diagonal class for a pair class");
+        launch(ctx->d_pairs.p + ctx->pc_off[pc], n, ctx->d_prims.p, ctx->boys.p, ctx->d_ratio.p,
+               ctx->d_Q.p + ctx->pc_off[pc], s);
+        QB_CUDA(ctx, cudaGetLastError());
     }
     QB_TRY(qb_check_status(ctx));
     std::vector<double> Q(npair);

@@ -400,12 +400,48 @@ __global__ void __launch_bounds__(32 * WPB) qb_jk_warp_kernel(const ClassWork w,
 // Variant 0 runs one contracted quartet per thread (qb_jk_class_kernel); variants 1..3
 // are configurations of the warp-cooperative kernel (null where not compiled).
 #define QB_NVARIANT 4
+typedef void (*QbSchwarzLaunch)(const ShellPair* pairs, int n, const PrimPair* prims, const double* boys,
+                                const double* ratio, double* Q, cudaStream_t s);
 struct ClassLaunchers {
     void (*jk[QB_NVARIANT])(const ClassWork&, const JKArgs&, int grid, cudaStream_t);
     int (*occupancy[QB_NVARIANT])(void);   // resident blocks per SM (also sets the shared-memory limit)
     int la, lb, lc, ld;
     int preferred;                         // default variant
+    QbSchwarzLaunch schwarz;               // diagonal classes (ab|ab): Schwarz factors of pair class (a, b)
 };
+
+// Schwarz factors Q_ab = max over components sqrt|(ab|ab)| of one pair class from the
+// class's own quartet code: the shell integrals times the per-function ratios r_a r_b of
+// the basis weights (weights factor as ratio(function) x coefficient(primitive)).
+template <int LA, int LB>
+__global__ void __launch_bounds__(128) qb_schwarz_class_kernel(const ShellPair* __restrict__ pairs, int n,
+                                                               const PrimPair* __restrict__ prims,
+                                                               const double* __restrict__ boys,
+                                                               const double* __restrict__ ratio,
+                                                               double* __restrict__ Q) {
+    using C = EriClass<LA, LB, LA, LB>;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const ShellPair P = pairs[k];
+    double I[C::NINT];
+    unsigned cnt = 0;
+    C::block(prims + P.prim0, P.nprim, prims + P.prim0, P.nprim, P.ABx, P.ABy, P.ABz, P.ABx, P.ABy, P.ABz, boys, I,
+             cnt);
+    double mx = 0.0;
+    for (int x = 0; x < C::NA; ++x)
+        for (int y = 0; y < C::NB; ++y) {
+            const double r = __ldg(ratio + P.fa + x) * __ldg(ratio + P.fb + y);
+            mx = fmax(mx, fabs(I[((x * C::NB + y) * C::NA + x) * C::NB + y]) * r * r);
+        }
+    Q[k] = sqrt(mx);
+}
+
+#define QB_DEFINE_SCHWARZ_LAUNCHER(LA, LB)                                                                     \
+    static void qb_schwarz_launch_##LA##LB##LA##LB(const ShellPair* p, int n, const PrimPair* prims,           \
+                                                   const double* boys, const double* ratio, double* Q,         \
+                                                   cudaStream_t s) {                                           \
+        if (n > 0) qb_schwarz_class_kernel<LA, LB><<<(n + 127) / 128, 128, 0, s>>>(p, n, prims, boys, ratio, Q); \
+    }
 
 #define QB_DEFINE_LAUNCHERS(LA, LB, LC, LD)                                                                  \
     static void qb_jk_launch_##LA##LB##LC##LD(const ClassWork& w, const JKArgs& a, int grid, cudaStream_t s) { \

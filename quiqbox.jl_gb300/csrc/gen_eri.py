@@ -477,8 +477,12 @@ def main(outdir, lmax=LMAX_DEFAULT):
                 jk.append("nullptr")
                 occ.append("nullptr")
         pref = PREFERRED.get(name, 1 if 1 in cfgs else 0)
+        schwarz = "nullptr"
+        if (la, lb) == (lc, ld):
+            cu.append(f"QB_DEFINE_SCHWARZ_LAUNCHER({la}, {lb})")
+            schwarz = f"qb_schwarz_launch_{name}"
         cu.append(f"ClassLaunchers qb_class_{name}() {{ return {{{{{', '.join(jk)}}}, {{{', '.join(occ)}}}, "
-                  f"{la}, {lb}, {lc}, {ld}, {pref}}}; }}")
+                  f"{la}, {lb}, {lc}, {ld}, {pref}, {schwarz}}}; }}")
         (outdir / f"eri_class_{name}.cu").write_text("\n".join(cu) + "\n")
         files.append(name)
         table[name] = {"prim_flops": g.prim.flops(), "contr_flops": g.contr.flops(),

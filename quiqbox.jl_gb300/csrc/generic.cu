@@ -398,23 +398,6 @@ __global__ void qb_eri_list_kernel(const GenBasis b, const double* __restrict__ 
     out[q] = md_eri(b, t[0], t[1], t[2], t[3], boys, status);
 }
 
-// Schwarz factors of a list of shell pairs (A, B) with na x nb functions:
-// Q = sqrt(max_{a in A, b in B} |(ab|ab)|).
-__global__ void qb_schwarz_generic_kernel(const GenBasis b, const double* __restrict__ boys,
-                                          const ShellPair* __restrict__ pairs, int n, int na, int nb,
-                                          double* __restrict__ Q, int* status) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const ShellPair P = pairs[k];
-    double mx = 0.0;
-    for (int x = 0; x < na; ++x)
-        for (int y = 0; y < nb; ++y) {
-            const int fa = P.fa + x, fb = P.fb + y;
-            mx = fmax(mx, fabs(md_eri(b, fa, fb, fa, fb, boys, status)));
-        }
-    Q[k] = sqrt(mx);
-}
-
 // Adjoint (backward) pass of the two-electron energy: functions [n, n + ng) of the
 // basis are extra single primitives g (derivatives of the basis functions' primitives),
 // functions [0, n) the basis itself with the total density P (n x n).  For every g, every
@@ -506,13 +489,6 @@ int qb_gen_eri_list(const GenDevBasis& gb, const double* boys, long long nq, con
     const int block = 64;
     const long long grid = (nq + block - 1) / block;
     if (grid > 0) qb_eri_list_kernel<<<(unsigned)grid, block, 0, s>>>(b, boys, nq, dq, out, status);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
-}
-
-int qb_gen_schwarz(const GenDevBasis& gb, const double* boys, const ShellPair* pairs, int n, int na, int nb,
-                   double* Q, int* status, cudaStream_t s) {
-    GenBasis b{gb.fp, gb.cen, gb.ijk, gb.alpha, gb.w, gb.nfun};
-    if (n > 0) qb_schwarz_generic_kernel<<<(n + 63) / 64, 64, 0, s>>>(b, boys, pairs, n, na, nb, Q, status);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

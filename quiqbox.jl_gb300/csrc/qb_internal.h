@@ -33,8 +33,6 @@ int qb_gen_onebody(const GenDevBasis& gb, int flags, int nnuc, const double* dZ,
 int qb_gen_eri(const GenDevBasis& gb, int mode, const double* boys, double* eri, const double* D, double* Jp,
                double* Kp, int* status, int nsm, cudaStream_t s);
 int qb_boys_device(int n, const double* dT, int M, int path, const double* boys, double* dout, cudaStream_t s);
-int qb_gen_schwarz(const GenDevBasis& gb, const double* boys, const ShellPair* pairs, int n, int na, int nb,
-                   double* Q, int* status, cudaStream_t s);
 int qb_gen_eri_list(const GenDevBasis& gb, const double* boys, long long nq, const int* dq, double* out,
                     int* status, cudaStream_t s);
 
