@@ -411,7 +411,7 @@ struct ClassLaunchers {
 };
 
 // Schwarz factors Q_ab = max over components sqrt|(ab|ab)| of one pair class from the
-// class's own quartet code: the shell integrals times the per-function ratios r_a r_b of
+// class's own quartet code with every primitive quartet: the shell integrals times the per-function ratios r_a r_b of
 // the basis weights (weights factor as ratio(function) x coefficient(primitive)).
 template <int LA, int LB>
 __global__ void __launch_bounds__(128) qb_schwarz_class_kernel(const ShellPair* __restrict__ pairs, int n,
@@ -425,8 +425,10 @@ __global__ void __launch_bounds__(128) qb_schwarz_class_kernel(const ShellPair* 
     const ShellPair P = pairs[k];
     double I[C::NINT];
     unsigned cnt = 0;
+    // every primitive quartet (no |K_ab K_cd| cut-off): a distant pair's (ab|ab) is tiny, yet
+    // Q_ab Q_cd with a compact (cd) can still pass the quartet threshold
     C::block(prims + P.prim0, P.nprim, prims + P.prim0, P.nprim, P.ABx, P.ABy, P.ABz, P.ABx, P.ABy, P.ABz, boys, I,
-             cnt);
+             cnt, 0.0);
     double mx = 0.0;
     for (int x = 0; x < C::NA; ++x)
         for (int y = 0; y < C::NB; ++y) {

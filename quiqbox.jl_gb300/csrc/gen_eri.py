@@ -380,17 +380,19 @@ class ClassGen:
         o += hrr
         o.append("  }")
         o.append("  // One contracted quartet in one thread: a flattened loop over the primitive quartets")
-        o.append("  // with |K_ab K_cd| >= QB_PRIM_EPS (pairs sorted by descending |K|), then the HRR.")
+        o.append("  // with |K_ab K_cd| >= eps (pairs sorted by descending |K|; eps = 0 evaluates all of")
+        o.append("  // them, as the Schwarz factors need), then the HRR.")
         o.append("  static __device__ __forceinline__ void block(")
         o.append("      const PrimPair* __restrict__ bp, int nbp, const PrimPair* __restrict__ kp, int nkp,")
         o.append("      double ABx, double ABy, double ABz, double CDx, double CDy, double CDz,")
-        o.append("      const double* __restrict__ boys_tab, double (&I)[NINT], unsigned& nprimq) {")
+        o.append("      const double* __restrict__ boys_tab, double (&I)[NINT], unsigned& nprimq,")
+        o.append("      const double eps = QB_PRIM_EPS) {")
         o.append("    double A[NT];")
         o.append("#pragma unroll")
         o.append("    for (int t = 0; t < NT; ++t) A[t] = 0.0;")
         o.append("    const double kmax_ket = nkp > 0 ? fabs(__ldg(&kp[0].K)) : 0.0;")
         o.append("    int ib = 0, ik = 0;")
-        o.append("    bool active = nbp > 0 && fabs(__ldg(&bp[0].K)) * kmax_ket >= QB_PRIM_EPS;")
+        o.append("    bool active = nbp > 0 && fabs(__ldg(&bp[0].K)) * kmax_ket >= eps;")
         o.append("    PrimPair B;")
         o.append("    if (active) B = qb_load_pair(bp);")
         o.append("    while (active) {")
@@ -398,10 +400,10 @@ class ClassGen:
         o.append("      ++nprimq;")
         o.append("      prim(B, Kt, boys_tab, [&](int t, double v) { A[t] += v; });")
         o.append("      ++ik;")
-        o.append("      if (ik >= nkp || fabs(B.K * __ldg(&kp[ik].K)) < QB_PRIM_EPS) {")
+        o.append("      if (ik >= nkp || fabs(B.K * __ldg(&kp[ik].K)) < eps) {")
         o.append("        ++ib;")
         o.append("        ik = 0;")
-        o.append("        if (ib >= nbp || fabs(__ldg(&bp[ib].K)) * kmax_ket < QB_PRIM_EPS) active = false;")
+        o.append("        if (ib >= nbp || fabs(__ldg(&bp[ib].K)) * kmax_ket < eps) active = false;")
         o.append("        else B = qb_load_pair(bp + ib);")
         o.append("      }")
         o.append("    }")

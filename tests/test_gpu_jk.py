@@ -73,6 +73,36 @@ def test_schwarz_screening_error_is_bounded(qb):
     assert np.abs(J1 - J0).max() < 1e-7 and np.abs(K1 - K0).max() < 1e-7
 
 
+def test_schwarz_factors_vs_exact_oracle(qb, oracle):
+    # the prepared pair table's Q_ab = sqrt(max |(ab|ab)|) against the quad-precision
+    # oracle, on a sparse 12-bohr box where many pairs are distant and diffuse (their
+    # (ab|ab) is tiny, but Q_ab Q_cd with a compact cd can still pass the threshold)
+    import ctypes as C
+    from quiqbox_gb300 import _lib as L
+    fb, _ = _small_shell_system(qb, 5, n_h=6, n_heavy=2, box=12.0)
+    ctx = qb.Context(0)
+    b = L.BasisArgs(fb)
+    ctx.check(ctx.lib.qb_jk_prepare(ctx.h, b.ref(), 1e-12))
+    npair = C.c_int()
+    ctx.check(ctx.lib.qb_jk_pair_table(ctx.h, C.byref(npair), None, None, None, None, None))
+    fa, fbb, la, lb = [np.zeros(npair.value, np.int32) for _ in range(4)]
+    Q = np.zeros(npair.value)
+    ctx.check(ctx.lib.qb_jk_pair_table(ctx.h, C.byref(npair), L.iptr(fa), L.iptr(fbb), L.iptr(la), L.iptr(lb),
+                                       L.dptr(Q)))
+    quartets, owner = [], []
+    for k in range(npair.value):
+        na, nb = (la[k] + 1) * (la[k] + 2) // 2, (lb[k] + 1) * (lb[k] + 2) // 2
+        for x in range(na):
+            for y in range(nb):
+                quartets.append((fa[k] + x, fbb[k] + y, fa[k] + x, fbb[k] + y))
+                owner.append(k)
+    vals = oracle.eri_list(fb, np.array(quartets, np.int32), exact=True)
+    Qr = np.zeros(npair.value)
+    np.maximum.at(Qr, np.array(owner), np.sqrt(np.abs(vals)))
+    assert (Qr < 1e-6).sum() > 10          # the box does have distant, diffuse pairs
+    assert np.all(np.abs(Q - Qr) <= 1e-10 * Qr + 1e-15)
+
+
 def test_benchmark_size_properties(qb):
     # 64 H + 16 heavy atoms, s/p/d, N = 416: symmetry, linearity and positivity of the Coulomb/exchange forms
     from quiqbox_gb300.workloads import random_shell_molecule, random_density
