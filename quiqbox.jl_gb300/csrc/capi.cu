@@ -58,7 +58,7 @@ int qb_create(qb_ctx** out, int device) {
         qb_get_class_launchers(ctx->launch);
         // Variant per class: the generator's measured preference.  QB_JK_VARIANT overrides
         // it for tuning: "thread" (variant 0 everywhere), "warp" (variant 1 wherever
-        // compiled), or one character per class, '0'..'3' (a variant that is not compiled
+        // compiled), or one character per class, '0'..'4' (a variant that is not compiled
         // for a class falls back to the preference).
         const char* ov = getenv("QB_JK_VARIANT");
         for (int c = 0; c < ctx->nclass; ++c) {

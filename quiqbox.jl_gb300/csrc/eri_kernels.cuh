@@ -178,6 +178,82 @@ struct QbRowSum {
     }
 };
 
+// Column k*stride of an owner's S accumulator rows, summed (input of the bra HRR of one
+// ket component: targets are stored e-major, k = e * NF + f).
+template <int S>
+struct QbColumnSum {
+    const double* p;
+    int stride, row;
+    __device__ __forceinline__ double operator[](int k) const {
+        double v = p[k * stride];
+#pragma unroll
+        for (int s = 1; s < S; ++s) v += p[s * row + k * stride];
+        return v;
+    }
+};
+
+// J/K digestion of one (ab|cd) block held in shared memory (Ib[ab * NCD + cd]) by a whole
+// warp: every element of the six J'/K' blocks is summed by one lane over the other index
+// pair (no reduction between lanes), scaled by the degeneracy factor and added to the
+// global accumulators.  Same six products per integral as qb_jk_digest.
+template <class C>
+__device__ __forceinline__ void qb_jk_digest_warp(const ShellPair& P, const ShellPair& Q, double deg,
+                                                  const JKArgs& a, const double* Ib, int lane) {
+    constexpr int NA = C::NA, NB = C::NB, NC = C::NC, ND = C::ND, NCD = NC * ND;
+    const int N = a.nfun;
+    const double* __restrict__ D = a.D;
+    auto Dat = [&](int r, int c) { return __ldg(D + r + (size_t)N * c); };
+    auto I = [&](int x, int y, int z, int u) { return Ib[(x * NB + y) * NCD + z * ND + u]; };
+    for (int r = lane; r < NA * NB; r += 32) {   // J_ab = sum_cd (ab|cd) D_cd
+        const int x = r / NB, y = r % NB;
+        double s = 0.0;
+        for (int z = 0; z < NC; ++z)
+            for (int u = 0; u < ND; ++u) s = fma(Dat(Q.fa + z, Q.fb + u), I(x, y, z, u), s);
+        atomicAdd(a.Jp + (P.fa + x) + (size_t)N * (P.fb + y), deg * s);
+    }
+    for (int r = lane; r < NC * ND; r += 32) {   // J_cd = sum_ab (ab|cd) D_ab
+        const int z = r / ND, u = r % ND;
+        double s = 0.0;
+        for (int x = 0; x < NA; ++x)
+            for (int y = 0; y < NB; ++y) s = fma(Dat(P.fa + x, P.fb + y), I(x, y, z, u), s);
+        atomicAdd(a.Jp + (Q.fa + z) + (size_t)N * (Q.fb + u), deg * s);
+    }
+    for (int r = lane; r < NA * NC; r += 32) {   // K_ac = sum_bd (ab|cd) D_bd
+        const int x = r / NC, z = r % NC;
+        double s = 0.0;
+        for (int y = 0; y < NB; ++y)
+            for (int u = 0; u < ND; ++u) s = fma(Dat(P.fb + y, Q.fb + u), I(x, y, z, u), s);
+        atomicAdd(a.Kp + (P.fa + x) + (size_t)N * (Q.fa + z), deg * s);
+    }
+    for (int r = lane; r < NA * ND; r += 32) {   // K_ad = sum_bc (ab|cd) D_bc
+        const int x = r / ND, u = r % ND;
+        double s = 0.0;
+        for (int y = 0; y < NB; ++y)
+            for (int z = 0; z < NC; ++z) s = fma(Dat(P.fb + y, Q.fa + z), I(x, y, z, u), s);
+        atomicAdd(a.Kp + (P.fa + x) + (size_t)N * (Q.fb + u), deg * s);
+    }
+    for (int r = lane; r < NB * NC; r += 32) {   // K_bc = sum_ad (ab|cd) D_ad
+        const int y = r / NC, z = r % NC;
+        double s = 0.0;
+        for (int x = 0; x < NA; ++x)
+            for (int u = 0; u < ND; ++u) s = fma(Dat(P.fa + x, Q.fb + u), I(x, y, z, u), s);
+        atomicAdd(a.Kp + (P.fb + y) + (size_t)N * (Q.fa + z), deg * s);
+    }
+    for (int r = lane; r < NB * ND; r += 32) {   // K_bd = sum_ac (ab|cd) D_ac
+        const int y = r / ND, u = r % ND;
+        double s = 0.0;
+        for (int x = 0; x < NA; ++x)
+            for (int z = 0; z < NC; ++z) s = fma(Dat(P.fa + x, Q.fa + z), I(x, y, z, u), s);
+        atomicAdd(a.Kp + (P.fb + y) + (size_t)N * (Q.fb + u), deg * s);
+    }
+}
+
+// Shared memory of one warp of the cooperative epilogue: (ab|f) and (ab|cd) of one quartet.
+template <class C>
+struct QbCoop {
+    static constexpr int doubles = C::NA * C::NB * C::NF + C::NINT;
+};
+
 // Warp-cooperative variant: a warp takes G <= 32 contracted quartets (one per "owner"
 // lane 0..G-1) and pools all their significant primitive quartets, dealt out evenly over
 // its 32 lanes in level order (the s-th primitive quartet of every owner, then the
@@ -189,8 +265,12 @@ struct QbRowSum {
 // 0..S-2, alone on their row, add without atomics.  The owners finally sum their rows
 // and run the HRR and the J/K digestion.  Lane
 // utilisation no longer depends on how many primitive quartets survive the screening
-// per contracted quartet, and the accumulators leave the register file.
-template <int LA, int LB, int LC, int LD, int WPB, int G, int S, bool REGROUP, bool PLAIN>
+// per contracted quartet, and the accumulators leave the register file.  COOP: instead
+// of each owner lane running its own HRR and digestion (hundreds of integrals per lane,
+// spilled to local memory in the large classes), the warp takes the owners one at a
+// time: the bra HRR with lanes over the ket components, the ket HRR with lanes over the
+// bra function pairs, then qb_jk_digest_warp, all through shared memory.
+template <int LA, int LB, int LC, int LD, int WPB, int G, int S, bool REGROUP, bool PLAIN, bool COOP>
 __global__ void __launch_bounds__(32 * WPB) qb_jk_warp_kernel(const ClassWork w, const JKArgs a) {
     using C = EriClass<LA, LB, LC, LD>;
     static_assert(G >= 1 && G <= 32, "owners per warp");
@@ -211,7 +291,8 @@ __global__ void __launch_bounds__(32 * WPB) qb_jk_warp_kernel(const ClassWork w,
     const unsigned FULL = 0xffffffffu;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned lanes_below = (1u << lane) - 1u;
-    double* acc = qb_dyn_smem + (size_t)warp * S * ROW;
+    constexpr int PER_WARP = S * ROW + (COOP ? QbCoop<C>::doubles : 0);
+    double* acc = qb_dyn_smem + (size_t)warp * PER_WARP;
     const long long total = __ldg(w.offs + w.nbra);
     const long long stride = (long long)gridDim.x * WPB * G;
     const float eps = (float)QB_PRIM_EPS;
@@ -384,11 +465,34 @@ __global__ void __launch_bounds__(32 * WPB) qb_jk_warp_kernel(const ClassWork w,
             if (lane == 0) nprim_warp += N;
             __syncwarp();
         }
-        if (valid) {
-            double I[C::NINT];
-            C::hrr(QbRowSum<S>{acc + lane * NTP, ROW}, P.ABx, P.ABy, P.ABz, Q.ABx, Q.ABy, Q.ABz, I);
-            const double deg = (P.same ? 1.0 : 2.0) * (Q.same ? 1.0 : 2.0) * ((w.same && i == j) ? 1.0 : 2.0);
-            qb_jk_digest<C>(P, Q, deg, a, I);
+        if constexpr (COOP) {
+            constexpr int NAB = C::NA * C::NB, NCD = C::NC * C::ND, NF = C::NF;
+            double* Tb = acc + S * ROW;   // (ab|f) of the current owner, [ab][f]
+            double* Ib = Tb + NAB * NF;   // (ab|cd), [ab][cd]
+            const unsigned vmask = __ballot_sync(FULL, valid);   // owners 0..popc-1 (consecutive quartets)
+            const int nown = __popc(vmask);
+            for (int g = 0; g < nown; ++g) {
+                const int ig = __shfl_sync(FULL, i, g), jg = __shfl_sync(FULL, j, g);
+                const ShellPair Pg = w.bra[ig];
+                const ShellPair Qg = w.ket[jg];
+                for (int f = lane; f < NF; f += 32)
+                    C::hrr_bra(QbColumnSum<S>{acc + g * NTP + f, NF, ROW}, Pg.ABx, Pg.ABy, Pg.ABz,
+                               [&](int ab, double v) { Tb[ab * NF + f] = v; });
+                __syncwarp();
+                for (int ab = lane; ab < NAB; ab += 32)
+                    C::hrr_ket(Tb + ab * NF, Qg.ABx, Qg.ABy, Qg.ABz, [&](int cd, double v) { Ib[ab * NCD + cd] = v; });
+                __syncwarp();
+                const double deg = (Pg.same ? 1.0 : 2.0) * (Qg.same ? 1.0 : 2.0) * ((w.same && ig == jg) ? 1.0 : 2.0);
+                qb_jk_digest_warp<C>(Pg, Qg, deg, a, Ib, lane);
+                __syncwarp();
+            }
+        } else {
+            if (valid) {
+                double I[C::NINT];
+                C::hrr(QbRowSum<S>{acc + lane * NTP, ROW}, P.ABx, P.ABy, P.ABz, Q.ABx, Q.ABy, Q.ABz, I);
+                const double deg = (P.same ? 1.0 : 2.0) * (Q.same ? 1.0 : 2.0) * ((w.same && i == j) ? 1.0 : 2.0);
+                qb_jk_digest<C>(P, Q, deg, a, I);
+            }
         }
         __syncwarp();
     }
@@ -399,7 +503,7 @@ __global__ void __launch_bounds__(32 * WPB) qb_jk_warp_kernel(const ClassWork w,
 // Host-side launchers, one set per class (defined in the generated eri_class_*.cu).
 // Variant 0 runs one contracted quartet per thread (qb_jk_class_kernel); variants 1..3
 // are configurations of the warp-cooperative kernel (null where not compiled).
-#define QB_NVARIANT 4
+#define QB_NVARIANT 5
 typedef void (*QbSchwarzLaunch)(const ShellPair* pairs, int n, const PrimPair* prims, const double* boys,
                                 const double* ratio, double* Q, cudaStream_t s);
 struct ClassLaunchers {
@@ -455,22 +559,24 @@ __global__ void __launch_bounds__(128) qb_schwarz_class_kernel(const ShellPair* 
         return nb;                                                                                           \
     }
 
-#define QB_WARP_SMEM(LA, LB, LC, LD, WPB, G, S) \
-    ((size_t)(WPB) * (S) * (G) * (EriClass<LA, LB, LC, LD>::NT | 1) * sizeof(double))
+#define QB_WARP_SMEM(LA, LB, LC, LD, WPB, G, S, COOP)                                   \
+    ((size_t)(WPB) * ((S) * (G) * (EriClass<LA, LB, LC, LD>::NT | 1) +                     \
+                      ((COOP) ? QbCoop<EriClass<LA, LB, LC, LD>>::doubles : 0)) * sizeof(double))
 
 // Warp-kernel configuration V of class LA LB LC LD.
-#define QB_DEFINE_WARP_LAUNCHERS(V, LA, LB, LC, LD, WPB, G, S, RG, PL)                                       \
+#define QB_DEFINE_WARP_LAUNCHERS(V, LA, LB, LC, LD, WPB, G, S, RG, PL, CO)                                   \
     static void qb_jkw##V##_launch_##LA##LB##LC##LD(const ClassWork& w, const JKArgs& a, int grid,          \
                                                     cudaStream_t s) {                                        \
-        qb_jk_warp_kernel<LA, LB, LC, LD, WPB, G, S, RG, PL>                                                 \
-            <<<grid, 32 * (WPB), QB_WARP_SMEM(LA, LB, LC, LD, WPB, G, S), s>>>(w, a);                        \
+        qb_jk_warp_kernel<LA, LB, LC, LD, WPB, G, S, RG, PL, CO>                                             \
+            <<<grid, 32 * (WPB), QB_WARP_SMEM(LA, LB, LC, LD, WPB, G, S, CO), s>>>(w, a);                    \
     }                                                                                                        \
     static int qb_occw##V##_##LA##LB##LC##LD(void) {                                                         \
-        cudaFuncSetAttribute(qb_jk_warp_kernel<LA, LB, LC, LD, WPB, G, S, RG, PL>,                            \
+        cudaFuncSetAttribute(qb_jk_warp_kernel<LA, LB, LC, LD, WPB, G, S, RG, PL, CO>,                        \
                              cudaFuncAttributeMaxDynamicSharedMemorySize,                                    \
-                             (int)QB_WARP_SMEM(LA, LB, LC, LD, WPB, G, S));                                  \
+                             (int)QB_WARP_SMEM(LA, LB, LC, LD, WPB, G, S, CO));                              \
         int nb = 0;                                                                                          \
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, qb_jk_warp_kernel<LA, LB, LC, LD, WPB, G, S, RG, PL>, \
-                                                      32 * (WPB), QB_WARP_SMEM(LA, LB, LC, LD, WPB, G, S));  \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb,                                                   \
+                                                      qb_jk_warp_kernel<LA, LB, LC, LD, WPB, G, S, RG, PL, CO>, \
+                                                      32 * (WPB), QB_WARP_SMEM(LA, LB, LC, LD, WPB, G, S, CO)); \
         return nb;                                                                                           \
     }

@@ -283,6 +283,50 @@ class ClassGen:
                         out.append(f"{ind}I[{k}] = {kname(a, b, cc, dd)};")
                         k += 1
 
+    def emit_hrr_split(self, o):
+        """The HRR as two one-dimensional transforms for the warp-cooperative epilogue:
+        hrr_bra maps one ket component's column of contracted targets (e0|f) (e in esets
+        order) to (ab|f); hrr_ket maps one bra function pair's row (ab|f0) (f in fsets
+        order) to (ab|cd).  Same recursions and operation order as emit_hrr."""
+        la, lb, lc, ld = self.la, self.lb, self.lc, self.ld
+
+        def nodes(pairs):
+            need = set()
+            stack = list(pairs)
+            while stack:
+                n = stack.pop()
+                if n in need:
+                    continue
+                need.add(n)
+                a, b = n
+                if sum(b) > 0:
+                    i = pick_axis(b)
+                    stack += [(add(a, i), sub(b, i)), (a, sub(b, i))]
+            return sorted(need, key=lambda n: (sum(n[1]), n))
+
+        for side, (l1, l2, src, D) in (("bra", (la, lb, self.esets, "AB")), ("ket", (lc, ld, self.fsets, "CD"))):
+            outs = [(x, y) for x in comps(l1) for y in comps(l2)]
+            nd = nodes(outs)
+
+            def nm(x, y):
+                return f"v{tname(x)}" if sum(y) == 0 else f"h{tname(x)}{tname(y)}"
+            used = {x for (x, y) in nd if sum(y) == 0}
+            o.append(f"  template <class In, class Out>")
+            o.append(f"  static __device__ __forceinline__ void hrr_{side}(const In& in, double {D}x, double {D}y, "
+                     f"double {D}z, Out&& out) {{")
+            for k, e in enumerate(src):
+                if e in used:
+                    o.append(f"    const double {nm(e, (0, 0, 0))} = in[{k}];")
+            for (x, y) in nd:
+                if sum(y) == 0:
+                    continue
+                i = pick_axis(y)
+                y1 = sub(y, i)
+                o.append(f"    const double {nm(x, y)} = fma({D}{AXES[i]}, {nm(x, y1)}, {nm(add(x, i), y1)});")
+            for k, (x, y) in enumerate(outs):
+                o.append(f"    out({k}, {nm(x, y)});")
+            o.append("  }")
+
     # -- Boys / quartet setup ----------------------------------------------------
     def emit_quartet_setup(self, out, ind, used_m, o2q, o2pq):
         c = self.prim
@@ -346,7 +390,8 @@ class ClassGen:
         o.append(f"// class ({la}{lb}|{lc}{ld}): {len(self.esets)}x{len(self.fsets)} contracted "
                  f"[e0|f0], {nint} integrals")
         o.append(f"template <> struct EriClass<{la}, {lb}, {lc}, {ld}> {{")
-        o.append(f"  static constexpr int NA = {na}, NB = {nb}, NC = {nc}, ND = {nd}, NINT = {nint}, NT = {nt};")
+        o.append(f"  static constexpr int NA = {na}, NB = {nb}, NC = {nc}, ND = {nd}, NINT = {nint}, NT = {nt}, "
+                 f"NE = {len(self.esets)}, NF = {len(self.fsets)};")
         o.append("  // VRR targets [e0|f0]^(0) of one primitive quartet (bra pair B, ket pair Kt), prefactor")
         o.append("  // included: sink(k, value) receives target k (in (e, f) order) as soon as it is final.")
         o.append("  template <class Sink>")
@@ -379,6 +424,8 @@ class ClassGen:
                 k += 1
         o += hrr
         o.append("  }")
+        o.append("  // The same HRR as two one-dimensional transforms (warp-cooperative epilogue).")
+        self.emit_hrr_split(o)
         o.append("  // One contracted quartet in one thread: a flattened loop over the primitive quartets")
         o.append("  // with |K_ab K_cd| >= eps (pairs sorted by descending |K|; eps = 0 evaluates all of")
         o.append("  // them, as the Schwarz factors need), then the HRR.")
@@ -425,23 +472,42 @@ SMEM_PER_WARP = 50 * 1024
 
 # Default variant per class (0: per-thread kernel), measured on GB300 with the J/K build
 # of 64 H + 16 C/N/O, 3-primitive s/p/d shells.  Classes not listed use variant 1.
-PREFERRED = {"2121": 0, "2211": 0, "2221": 0,
+PREFERRED = {"2211": 0, "2221": 0, "2111": 4, "2121": 4, "2220": 4, "2222": 4,
              "0000": 2, "1000": 2, "1010": 2, "1100": 2, "2000": 2, "2010": 2, "2100": 2,
              "1110": 3, "2020": 3}
 
 
-def warp_configs(nt):
-    """{variant: (G, S, regroup, plain)} of the warp kernel for a class with NT targets."""
+COOP_MIN_NINT = 324   # classes with at least this many integrals get the cooperative epilogue
+BIG_NT = 90           # classes with at least this many contracted targets get variant 4
+SMEM_PER_WARP_8 = 24 * 1024   # variant 4 with 8 warps per block (two per SM sub-partition)
+
+
+def warp_configs(nt, nint=0, nab=0, nf=0):
+    """{variant: (G, S, regroup, plain, coop, warps per block)} of the warp kernel for a
+    class with NT targets.  Variant 4, for the classes whose accumulators fill shared
+    memory at four warps per block: eight warps per block with half the shared memory per
+    warp (more warps to hide the FP64 and shared-memory latencies), four where that
+    leaves fewer than two owners; coop (classes of >= 324 integrals): the whole warp runs
+    each owner's HRR and J/K digestion from shared memory."""
     rows = SMEM_PER_WARP // ((nt | 1) * 8)
-    if rows < 1:
-        return {}
-    if rows < 32:
-        return {1: (rows, 1, False, False)}
-    cfg = {1: (32, 1, False, False)}
-    s_max = min(4, rows // 32)
-    if s_max >= 2:
-        cfg[2] = (32, s_max, True, True)
-        cfg[3] = (32, 2, True, False)
+    cfg = {}
+    if rows >= 1:
+        if rows < 32:
+            cfg[1] = (rows, 1, False, False, False, WARPS_PER_BLOCK)
+        else:
+            cfg[1] = (32, 1, False, False, False, WARPS_PER_BLOCK)
+            s_max = min(4, rows // 32)
+            if s_max >= 2:
+                cfg[2] = (32, s_max, True, True, False, WARPS_PER_BLOCK)
+                cfg[3] = (32, 2, True, False, False, WARPS_PER_BLOCK)
+    if nt >= BIG_NT:
+        coop = nint >= COOP_MIN_NINT
+        extra = nab * nf + nint if coop else 0
+        for per_warp, wpb in ((SMEM_PER_WARP_8, 8), (SMEM_PER_WARP, WARPS_PER_BLOCK)):
+            g = (per_warp // 8 - extra) // (nt | 1)
+            if g >= 2 or (wpb == WARPS_PER_BLOCK and g >= 1):
+                cfg[4] = (min(32, g), 1, False, False, coop, wpb)
+                break
     return cfg
 
 
@@ -463,16 +529,18 @@ def main(outdir, lmax=LMAX_DEFAULT):
         (outdir / f"eri_class_{name}.cuh").write_text(HEADER + code + "\n")
         la, lb, lc, ld = cls
         nt = len(g.esets) * len(g.fsets)
-        cfgs = warp_configs(nt)
+        nint_c = ncart(la) * ncart(lb) * ncart(lc) * ncart(ld)
+        cfgs = warp_configs(nt, nint_c, ncart(la) * ncart(lb), len(g.fsets))
         cu = [f'// GENERATED by gen_eri.py -- do not edit.',
               f'#include "eri_class_{name}.cuh"', '#include "eri_kernels.cuh"',
               f'QB_DEFINE_LAUNCHERS({la}, {lb}, {lc}, {ld})']
         jk, occ = [f"qb_jk_launch_{name}"], [f"qb_occ_{name}"]
-        for v in (1, 2, 3):
+        for v in (1, 2, 3, 4):
             if v in cfgs:
-                G_, S_, rg, pl = cfgs[v]
-                cu.append(f"QB_DEFINE_WARP_LAUNCHERS({v}, {la}, {lb}, {lc}, {ld}, {WARPS_PER_BLOCK}, {G_}, {S_}, "
-                          f"{'true' if rg else 'false'}, {'true' if pl else 'false'})")
+                G_, S_, rg, pl, co, wpb = cfgs[v]
+                cu.append(f"QB_DEFINE_WARP_LAUNCHERS({v}, {la}, {lb}, {lc}, {ld}, {wpb}, {G_}, {S_}, "
+                          f"{'true' if rg else 'false'}, {'true' if pl else 'false'}, "
+                          f"{'true' if co else 'false'})")
                 jk.append(f"qb_jkw{v}_launch_{name}")
                 occ.append(f"qb_occw{v}_{name}")
             else:
