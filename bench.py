@@ -471,10 +471,11 @@ def learned_guess(qb, n_mol):
     core-Hamiltonian fallback for the ones it does not converge)."""
     from quiqbox_gb300 import guess, _lib as L
     net = guess.load(L.load())
+    meta = json.loads(str(np.load(guess.WEIGHTS_FILE)["meta"]))
     ev = guess.evaluate(qb, net, n_mol, seed=202)
     ev["workload"] = ("held-out seeded chains of 3-12 atoms (H:C:N:O = 5:3:1:1), STO-3G, neutral or +1; "
                       "batched RHF, DIIS, |dE| <= 1e-10, RMS(dD) <= 1e-8; network: 4 x 256 GELU MLP, "
-                      "BF16 weights, FP32 accumulation, trained on 19 038 molecules")
+                      f"BF16 weights, FP32 accumulation, trained on {meta['n_train_molecules']} molecules")
     return ev
 
 
