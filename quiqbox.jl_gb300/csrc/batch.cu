@@ -46,6 +46,7 @@
 #define QB_BATCH_RESET 4e-13               // resetThreshold = 1000 getAtolVal(Float64) (HartreeFock.jl:1337)
 #define QB_BATCH_NCLASS 6
 #define QB_BATCH_THREADS 256
+#define QB_STEP_SMEM 12000     // doubles of dynamic shared memory of the step kernel (two blocks per SM)
 
 namespace {
 
@@ -191,60 +192,71 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_orth_kernel(MolDev*
 // Pulay DIIS coefficients c (m entries) from the error Gram matrix B (ld QB_BATCH_SLOTS) of
 // the slots in idx: minimise c^T B c subject to sum c = 1 (DIIScore with v = 0,
 // HartreeFock.jl:1301-1315; the minimiser the constraint solvers converge to) via the
-// bordered linear system, Gaussian elimination with partial pivoting (one thread).
-// Returns false if singular.
-__device__ bool qb_diis_coeffs(int m, const double* B, const int* idx, double* c) {
-    double A[(QB_BATCH_SLOTS + 1) * (QB_BATCH_SLOTS + 1)], b[QB_BATCH_SLOTS + 1];
-    const int n = m + 1;
+// bordered linear system, Gaussian elimination with partial pivoting (largest |pivot|,
+// lowest row on ties; singular below 1e-14 after scaling by max B_ii) by one warp: lane i
+// holds row i in shared memory A and the rows of each elimination step update in
+// parallel.  Every lane of the warp calls it; the result is warp-uniform; false if singular.
+__device__ bool qb_diis_coeffs_warp(int m, const double* B, const int* idx, double* c,
+                                    double (*A)[QB_BATCH_SLOTS + 2]) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, n = m + 1;
     double scale = 0.0;
     for (int i = 0; i < m; ++i) scale = fmax(scale, fabs(B[idx[i] * QB_BATCH_SLOTS + idx[i]]));
     if (!(scale > 0.0)) return false;
-    for (int i = 0; i < m; ++i) {
-        for (int j = 0; j < m; ++j) A[i + n * j] = B[idx[i] * QB_BATCH_SLOTS + idx[j]] / scale;
-        A[i + n * m] = 1.0;
-        A[m + n * i] = 1.0;
-        b[i] = 0.0;
+    if (lane < n) {
+        for (int j = 0; j < n; ++j)
+            A[lane][j] = lane < m ? (j < m ? B[idx[lane] * QB_BATCH_SLOTS + idx[j]] / scale : 1.0) : (j < m ? 1.0 : 0.0);
+        A[lane][n] = lane < m ? 0.0 : 1.0;   // right-hand side
     }
-    A[m + n * m] = 0.0;
-    b[m] = 1.0;
+    __syncwarp();
     for (int k = 0; k < n; ++k) {
-        int piv = k;
-        for (int i = k + 1; i < n; ++i)
-            if (fabs(A[i + n * k]) > fabs(A[piv + n * k])) piv = i;
-        if (!(fabs(A[piv + n * k]) > 1e-14)) return false;
-        if (piv != k) {
-            for (int j = 0; j < n; ++j) {
-                const double t = A[k + n * j];
-                A[k + n * j] = A[piv + n * j];
-                A[piv + n * j] = t;
+        double v = (lane >= k && lane < n) ? fabs(A[lane][k]) : -1.0;
+        int pi = lane;
+        for (int o = 16; o > 0; o >>= 1) {
+            const double v2 = __shfl_xor_sync(FULL, v, o);
+            const int p2 = __shfl_xor_sync(FULL, pi, o);
+            if (v2 > v || (v2 == v && p2 < pi)) {
+                v = v2;
+                pi = p2;
             }
-            const double t = b[k];
-            b[k] = b[piv];
-            b[piv] = t;
         }
-        for (int i = k + 1; i < n; ++i) {
-            const double f = A[i + n * k] / A[k + n * k];
-            for (int j = k; j < n; ++j) A[i + n * j] -= f * A[k + n * j];
-            b[i] -= f * b[k];
+        if (!(v > 1e-14)) return false;
+        if (pi != k && lane <= n) {
+            const double t = A[k][lane];
+            A[k][lane] = A[pi][lane];
+            A[pi][lane] = t;
         }
+        __syncwarp();
+        if (lane > k && lane < n) {
+            const double f = A[lane][k] / A[k][k];
+            for (int j = k; j < n; ++j) A[lane][j] -= f * A[k][j];
+            A[lane][n] -= f * A[k][n];
+        }
+        __syncwarp();
     }
-    for (int i = n - 1; i >= 0; --i) {
-        double s = b[i];
-        for (int j = i + 1; j < n; ++j) s -= A[i + n * j] * b[j];
-        b[i] = s / A[i + n * i];
+    if (lane == 0) {
+        for (int i = n - 1; i >= 0; --i) {
+            double t = A[i][n];
+            for (int j = i + 1; j < n; ++j) t -= A[i][j] * A[j][n];
+            A[i][n] = t / A[i][i];
+        }
+        for (int i = 0; i < m; ++i) c[i] = A[i][n];
     }
-    for (int i = 0; i < m; ++i) c[i] = b[i];
+    __syncwarp();
     return true;
 }
 
 // One SCF iteration of one molecule per thread block (blocks ordered by size, largest first).
 __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev* mols, const int* __restrict__ order,
-                                                                         const StepParams prm, int* active) {
+                                                                         const StepParams prm, int* active,
+                                                                         int smem_doubles) {
+    extern __shared__ double s_work[];   // eigensolver workspace when the molecule fits
     __shared__ QbJacobiSmem<QB_BATCH_MAXN> jsm;
     __shared__ QbEigSmem<QB_BATCH_MAXN> esm;
     __shared__ double red[33];
     __shared__ double s_c[QB_BATCH_SLOTS];
     __shared__ int s_idx[QB_BATCH_SLOTS], s_ok;
+    __shared__ double s_diis[QB_BATCH_SLOTS][QB_BATCH_SLOTS + 2];
     MolDev& M = mols[order[blockIdx.x]];
     if (M.conv) return;
     const int n = M.n, nn = n * n, tid = threadIdx.x, nt = blockDim.x;
@@ -334,17 +346,23 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
             }
             const int m = M.dlen;
             for (int k = 0; k < m; ++k) s_idx[k] = M.dlist[k];
-            bool ok = true;
-            if (m == 1) s_c[0] = 1.0;
-            else ok = qb_diis_coeffs(m, M.B, s_idx, s_c);
-            if (!ok) {   // singular system: extrapolate with the newest entry only
-                for (int k = 0; k < m; ++k) s_c[k] = 0.0;
-                s_c[m - 1] = 1.0;
-            }
             s_ok = m;
         }
         __syncthreads();
         const int m = s_ok;
+        if (tid < 32) {   // Pulay coefficients by warp 0
+            bool ok = true;
+            if (m == 1) {
+                if (tid == 0) s_c[0] = 1.0;
+            } else {
+                ok = qb_diis_coeffs_warp(m, M.B, s_idx, s_c, s_diis);
+            }
+            if (!ok && tid == 0) {   // singular system: extrapolate with the newest entry only
+                for (int k = 0; k < m; ++k) s_c[k] = 0.0;
+                s_c[m - 1] = 1.0;
+            }
+        }
+        __syncthreads();
         for (int idx = tid; idx < nn; idx += nt) {
             double f = 0.0;
             for (int k = 0; k < m; ++k) f = fma(s_c[k], M.Fh[(size_t)s_idx[k] * nn + idx], f);
@@ -356,11 +374,24 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
     if (prm.eig == 0) {
         // occupied eigenvectors Y of F' (W1, n x nocc): Householder + bisection + inverse
         // iteration; D' = Y Y^T (W3) and D = (X Y)(X Y)^T (W2)
-        for (int i = tid; i < nn; i += nt) M.W3[i] = M.W2[i];
+        // (the matrix, vectors and LU factors in shared memory when they fit: the
+        // Householder steps and the triangular solves are latency-bound)
+        const int k = M.nocc;
+        const long long need = (long long)nn + 4LL * n * k + n;
+        double *Aw = M.W3, *Yw = M.W1, *B0 = M.W4, *B1 = M.W5, *B2 = M.W6, *pw = M.wt;
+        if (need <= smem_doubles) {
+            Aw = s_work;
+            Yw = Aw + nn;
+            B0 = Yw + (size_t)n * k;
+            B1 = B0 + (size_t)n * k;
+            B2 = B1 + (size_t)n * k;
+            pw = B2 + (size_t)n * k;
+        }
+        for (int i = tid; i < nn; i += nt) Aw[i] = M.W2[i];
         __syncthreads();
-        qb_cta_lowest_eig<QB_BATCH_MAXN>(n, M.nocc, M.W3, M.W1, M.eps, M.W4, M.W5, M.W6, M.wt, esm);
-        qb_cta_gemm(false, true, n, n, M.nocc, 1.0, M.W1, n, M.W1, n, 0.0, M.W3, n);
-        qb_cta_gemm(false, false, n, M.nocc, n, 1.0, M.X, n, M.W1, n, 0.0, M.W4, n);
+        qb_cta_lowest_eig<QB_BATCH_MAXN>(n, k, Aw, Yw, M.eps, B0, B1, B2, pw, esm);
+        qb_cta_gemm(false, true, n, n, k, 1.0, Yw, n, Yw, n, 0.0, M.W3, n);
+        qb_cta_gemm(false, false, n, k, n, 1.0, M.X, n, Yw, n, 0.0, M.W4, n);
         qb_cta_gemm(false, true, n, n, M.nocc, 1.0, M.W4, n, M.W4, n, 0.0, M.W2, n);
     } else {
         // rotate into the previous eigenvectors, A = C'^T F' C' (W3), and diagonalise;
@@ -810,6 +841,14 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
                          cfg.jacobi_sweeps > 0 ? std::min(cfg.jacobi_sweeps, 60) : 60, cfg.eigensolver ? 1 : 0,
                          cfg.initial_density && cfg.fallback_iter > 0 ? cfg.fallback_iter : 0};
     int* d_active = d_counters.p + 1;
+    // eigensolver workspace in shared memory: the largest molecule's n^2 + 4 n nocc + n
+    // doubles, at most QB_STEP_SMEM (two blocks per SM still fit)
+    long long step_need = 0;
+    for (int m = 0; m < nmol; ++m)
+        step_need = std::max(step_need, (long long)nf[m] * nf[m] + 4LL * nf[m] * nocc[m] + nf[m]);
+    const int step_smem = (int)std::min<long long>(step_need, QB_STEP_SMEM);
+    QB_CUDA(ctx, cudaFuncSetAttribute(qb_batch_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(QB_STEP_SMEM * sizeof(double))));
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     QB_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -820,7 +859,8 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
             if (nch == 0) continue;
             kClasses[c].digest(work[c], d_chunks.p + chunk_at[c], d_eri.p + eri_at[c], d_mols.p, nch, s);
         }
-        qb_batch_step_kernel<<<nmol, QB_BATCH_THREADS, 0, s>>>(d_mols.p, d_order.p, prm, d_active);
+        qb_batch_step_kernel<<<nmol, QB_BATCH_THREADS, step_smem * sizeof(double), s>>>(d_mols.p, d_order.p, prm,
+                                                                                     d_active, step_smem);
     }
     const cudaError_t cap = cudaStreamEndCapture(s, &graph);
     QB_CUDA(ctx, cap);

@@ -392,24 +392,33 @@ __device__ void qb_cta_lowest_eig(int n, int k, double* A, double* Y, double* w,
                 frozen = !(hi - lo > 2.4e-7f * fmaxf(fabsf(lo), fabsf(hi)) + absres);
             }
         }
+        if (i < k && sub == 0) sm.lam[i] = 0.5 * ((double)lo + (double)hi);
+    }
+    __syncthreads();
+    // inverse iteration at the fixed FP32 shift (within ~1e-7 ||T|| of the eigenvalue):
+    // components of eigenvalues further than 1e-4 ||T|| shrink by >= 1e3 per step, so four
+    // steps leave <= 1e-12 of them; an eigenvalue within 1e-4 ||T|| of a neighbour (a
+    // cluster, orthogonalised below) takes six, which also separates pairs whose shifts
+    // differ by a few FP32 ulps
+    for (int i0 = 0; i0 < k; i0 += ngrp) {
+        const int i = i0 + tid / G;
         if (i < k && sub == 0) {
-            const double lam = 0.5 * ((double)lo + (double)hi);
+            const double lam = sm.lam[i];
+            const bool clustered = (i > 0 && lam - sm.lam[i - 1] <= 1e-4 * nrm) ||
+                                   (i + 1 < k && sm.lam[i + 1] - lam <= 1e-4 * nrm);
             double* y = Yt + i;
             for (int j = 0; j < n; ++j) {   // deterministic start vector, distinct per eigenvalue
                 const unsigned h = (unsigned)(j * 2654435761u) ^ (unsigned)(i * 40503u + 17u);
                 y[(size_t)k * j] = 1.0 + 0.25 * ((double)(h & 0xffff) / 65536.0 - 0.5);
             }
-            // inverse iteration at the fixed FP32 shift (within ~1e-7 ||T|| of the eigenvalue):
-            // components of eigenvalues further than 1e-4 ||T|| shrink by >= 1e3 per step
             qb_tridiag_factor(n, sm.d, sm.e, lam, pert, B1 + i, B2 + i, Y + i, k);
-            for (int s = 0; s < 6; ++s) {
+            for (int s = 0; s < (clustered ? 6 : 4); ++s) {
                 qb_tridiag_apply(n, sm.e, B1 + i, B2 + i, Y + i, y, k);
                 double nn2 = 0.0;
                 for (int j = 0; j < n; ++j) nn2 = fma(y[(size_t)k * j], y[(size_t)k * j], nn2);
                 const double inv = 1.0 / sqrt(nn2);
                 for (int j = 0; j < n; ++j) y[(size_t)k * j] *= inv;
             }
-            sm.lam[i] = lam;
         }
     }
     __syncthreads();
