@@ -382,6 +382,33 @@ class BatchSCFResult:
     restarted: Optional[np.ndarray] = None   # restarted from the core-Hamiltonian guess (fallback_iter)
 
 
+_TRIU = {}
+
+
+def _nuc_repulsions(nnuc, Z, R):
+    """nucRepulsion (src/Particles.jl:197-210) of every molecule of a batch at once:
+    nuclei concatenated (charges Z, positions R, nnuc per molecule)."""
+    nnuc = np.asarray(nnuc, np.int64)
+    start = np.concatenate([[0], np.cumsum(nnuc)[:-1]])
+    ii, jj, mol = [], [], []
+    for m, (n, s) in enumerate(zip(nnuc, start)):
+        if n < 2:
+            continue
+        t = _TRIU.get(n)
+        if t is None:
+            t = _TRIU[n] = np.triu_indices(n, 1)
+        ii.append(t[0] + s)
+        jj.append(t[1] + s)
+        mol.append(np.full(len(t[0]), m))
+    out = np.zeros(len(nnuc))
+    if ii:
+        i, j, mol = np.concatenate(ii), np.concatenate(jj), np.concatenate(mol)
+        P = R.reshape(-1, 3)
+        d = np.sqrt(np.sum((P[i] - P[j]) ** 2, axis=1))
+        out = np.bincount(mol, weights=Z[i] * Z[j] / d, minlength=len(nnuc))
+    return out
+
+
 def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ctx=None,
                           initial_densities=None, return_densities=False) -> BatchSCFResult:
     """Closed-shell HF of many molecules in one call (qb_run_rhf_batched).
@@ -407,12 +434,12 @@ def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ct
         Zs.append(Zm)
         Rs.append(nuc.positions.reshape(-1))
         nocc.append(nel // 2)
-        enn.append(nucRepulsion(nuc))
         nf.append(fb.nfun)
     bases = (L.QBBasis * nmol)(*[a.s for a in args])
     nnuc_a = np.ascontiguousarray(nnuc, np.int32)
     Z = np.ascontiguousarray(np.concatenate(Zs), np.float64)
     R = np.ascontiguousarray(np.concatenate(Rs), np.float64)
+    enn = _nuc_repulsions(nnuc_a, Z, R)
     nocc_a = np.ascontiguousarray(nocc, np.int32)
     d0 = None
     d0_dev = None
@@ -451,7 +478,7 @@ def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ct
         for n in nf:
             dens.append(dout[off:off + n * n].reshape((n, n), order="F"))
             off += n * n
-    return BatchSCFResult(E + np.array(enn), E, it, conv.astype(bool), sw, np.array(nf), res.ms_integrals,
+    return BatchSCFResult(E + enn, E, it, conv.astype(bool), sw, np.array(nf), res.ms_integrals,
                           res.ms_scf, int(res.quartets), int(res.prim_quartets), int(res.eri_doubles),
                           int(res.graph_launches), dens, rst.astype(bool))
 

@@ -208,12 +208,13 @@ class NuclearCluster:
 
 def nucRepulsion(nuc: NuclearCluster) -> float:
     """nucRepulsion (src/Particles.jl:197-210)."""
-    Z, R = nuc.charges, nuc.positions
-    res = 0.0
-    for i in range(len(Z)):
-        for j in range(i + 1, len(Z)):
-            res += Z[i] * Z[j] / float(np.linalg.norm(R[i] - R[j]))
-    return res
+    Z = np.asarray(nuc.charges, dtype=np.float64)
+    R = np.asarray(nuc.positions, dtype=np.float64).reshape(-1, 3)
+    if len(Z) < 2:
+        return 0.0
+    i, j = np.triu_indices(len(Z), 1)
+    d = np.sqrt(np.sum((R[i] - R[j]) ** 2, axis=1))
+    return float(np.sum(Z[i] * Z[j] / d))
 
 
 @dataclass
