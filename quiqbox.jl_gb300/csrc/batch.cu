@@ -46,7 +46,6 @@
 #define QB_BATCH_RESET 4e-13               // resetThreshold = 1000 getAtolVal(Float64) (HartreeFock.jl:1337)
 #define QB_BATCH_NCLASS 6
 #define QB_BATCH_THREADS 256
-#define QB_STEP_SMEM 12000     // doubles of dynamic shared memory of the step kernel (two blocks per SM)
 
 namespace {
 
@@ -248,9 +247,7 @@ __device__ bool qb_diis_coeffs_warp(int m, const double* B, const int* idx, doub
 
 // One SCF iteration of one molecule per thread block (blocks ordered by size, largest first).
 __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev* mols, const int* __restrict__ order,
-                                                                         const StepParams prm, int* active,
-                                                                         int smem_doubles) {
-    extern __shared__ double s_work[];   // eigensolver workspace when the molecule fits
+                                                                         const StepParams prm, int* active) {
     __shared__ QbJacobiSmem<QB_BATCH_MAXN> jsm;
     __shared__ QbEigSmem<QB_BATCH_MAXN> esm;
     __shared__ double red[33];
@@ -374,22 +371,11 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
     if (prm.eig == 0) {
         // occupied eigenvectors Y of F' (W1, n x nocc): Householder + bisection + inverse
         // iteration; D' = Y Y^T (W3) and D = (X Y)(X Y)^T (W2)
-        // (the matrix, vectors and LU factors in shared memory when they fit: the
-        // Householder steps and the triangular solves are latency-bound)
         const int k = M.nocc;
-        const long long need = (long long)nn + 4LL * n * k + n;
-        double *Aw = M.W3, *Yw = M.W1, *B0 = M.W4, *B1 = M.W5, *B2 = M.W6, *pw = M.wt;
-        if (need <= smem_doubles) {
-            Aw = s_work;
-            Yw = Aw + nn;
-            B0 = Yw + (size_t)n * k;
-            B1 = B0 + (size_t)n * k;
-            B2 = B1 + (size_t)n * k;
-            pw = B2 + (size_t)n * k;
-        }
+        double *Aw = M.W3, *Yw = M.W1;
         for (int i = tid; i < nn; i += nt) Aw[i] = M.W2[i];
         __syncthreads();
-        qb_cta_lowest_eig<QB_BATCH_MAXN>(n, k, Aw, Yw, M.eps, B0, B1, B2, pw, esm);
+        qb_cta_lowest_eig<QB_BATCH_MAXN>(n, k, Aw, Yw, M.eps, M.W4, M.W5, M.W6, M.wt, esm);
         qb_cta_gemm(false, true, n, n, k, 1.0, Yw, n, Yw, n, 0.0, M.W3, n);
         qb_cta_gemm(false, false, n, k, n, 1.0, M.X, n, Yw, n, 0.0, M.W4, n);
         qb_cta_gemm(false, true, n, n, M.nocc, 1.0, M.W4, n, M.W4, n, 0.0, M.W2, n);
@@ -841,14 +827,6 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
                          cfg.jacobi_sweeps > 0 ? std::min(cfg.jacobi_sweeps, 60) : 60, cfg.eigensolver ? 1 : 0,
                          cfg.initial_density && cfg.fallback_iter > 0 ? cfg.fallback_iter : 0};
     int* d_active = d_counters.p + 1;
-    // eigensolver workspace in shared memory: the largest molecule's n^2 + 4 n nocc + n
-    // doubles, at most QB_STEP_SMEM (two blocks per SM still fit)
-    long long step_need = 0;
-    for (int m = 0; m < nmol; ++m)
-        step_need = std::max(step_need, (long long)nf[m] * nf[m] + 4LL * nf[m] * nocc[m] + nf[m]);
-    const int step_smem = (int)std::min<long long>(step_need, QB_STEP_SMEM);
-    QB_CUDA(ctx, cudaFuncSetAttribute(qb_batch_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(QB_STEP_SMEM * sizeof(double))));
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     QB_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -859,8 +837,7 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
             if (nch == 0) continue;
             kClasses[c].digest(work[c], d_chunks.p + chunk_at[c], d_eri.p + eri_at[c], d_mols.p, nch, s);
         }
-        qb_batch_step_kernel<<<nmol, QB_BATCH_THREADS, step_smem * sizeof(double), s>>>(d_mols.p, d_order.p, prm,
-                                                                                     d_active, step_smem);
+        qb_batch_step_kernel<<<nmol, QB_BATCH_THREADS, 0, s>>>(d_mols.p, d_order.p, prm, d_active);
     }
     const cudaError_t cap = cudaStreamEndCapture(s, &graph);
     QB_CUDA(ctx, cap);
