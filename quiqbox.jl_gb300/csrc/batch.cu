@@ -87,15 +87,68 @@ struct StepParams {
 };
 
 // ---------------------------------------------------------------------------
+// Visiting order of a class's quartets for the store kernel: by primitive-pair product
+// (bucket 15 - floor(log2(nprim_bra * nprim_ket)), largest first), so that the lanes of a
+// warp evaluate quartets of similar primitive counts (mixed bases pair 1- and 36-primitive
+// shell pairs; a warp waits for its longest lane).  Counting sort: histogram, exclusive
+// scan, scatter (order within a bucket is arbitrary; every quartet keeps its own slot).
+#define QB_COST_BUCKETS 16
+__device__ __forceinline__ int qb_cost_bucket(const BatchWork& w, long long t) {
+    const int i = qb_find_bra(w.offs, w.nbra, t);
+    const int j = __ldg(w.kstart + i) + (int)(t - __ldg(w.offs + i));
+    const unsigned c = (unsigned)max(1, w.bra[i].nprim) * (unsigned)max(1, w.ket[j].nprim);
+    return QB_COST_BUCKETS - 1 - min(QB_COST_BUCKETS - 1, 31 - __clz(c));
+}
+
+__global__ void qb_batch_cost_hist_kernel(const BatchWork w, unsigned* __restrict__ hist) {
+    __shared__ unsigned h[QB_COST_BUCKETS];
+    if (threadIdx.x < QB_COST_BUCKETS) h[threadIdx.x] = 0;
+    __syncthreads();
+    const long long total = __ldg(w.offs + w.nbra);
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x)
+        atomicAdd(&h[qb_cost_bucket(w, t)], 1u);
+    __syncthreads();
+    if (threadIdx.x < QB_COST_BUCKETS && h[threadIdx.x]) atomicAdd(hist + threadIdx.x, h[threadIdx.x]);
+}
+
+__global__ void qb_batch_cost_scan_kernel(unsigned* hist) {   // counts -> exclusive prefix (one thread)
+    unsigned acc = 0;
+    for (int b = 0; b < QB_COST_BUCKETS; ++b) {
+        const unsigned v = hist[b];
+        hist[b] = acc;
+        acc += v;
+    }
+}
+
+__global__ void qb_batch_cost_scatter_kernel(const BatchWork w, unsigned* __restrict__ cursor,
+                                             unsigned* __restrict__ perm) {
+    const long long total = __ldg(w.offs + w.nbra);
+    const int lane = threadIdx.x & 31;
+    for (long long t0 = (long long)blockIdx.x * blockDim.x; t0 < total; t0 += (long long)gridDim.x * blockDim.x) {
+        const long long t = t0 + threadIdx.x;
+        const bool act = t < total;
+        const int b = act ? qb_cost_bucket(w, t) : QB_COST_BUCKETS + lane;   // inactive lanes: unique keys
+        const unsigned same = __match_any_sync(0xffffffffu, b);
+        const int leader = __ffs(same) - 1;
+        unsigned base = 0;
+        if (act && lane == leader) base = atomicAdd(cursor + b, (unsigned)__popc(same));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (act) perm[base + __popc(same & ((1u << lane) - 1u))] = (unsigned)t;
+    }
+}
+
+// ---------------------------------------------------------------------------
 template <int LA, int LB, int LC, int LD>
 __global__ void __launch_bounds__(128) qb_batch_store_kernel(const BatchWork w, const PrimPair* __restrict__ prims,
                                                              const double* __restrict__ boys, double* __restrict__ out,
-                                                             unsigned long long* primcount) {
+                                                             unsigned long long* primcount,
+                                                             const unsigned* __restrict__ perm) {
     using C = EriClass<LA, LB, LC, LD>;
     const long long total = __ldg(w.offs + w.nbra);
     const long long stride = (long long)gridDim.x * blockDim.x;
     unsigned nprimq = 0;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+    for (long long u = (long long)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += stride) {
+        const long long t = __ldg(perm + u);   // quartets visited in cost order, stored in place
         const int i = qb_find_bra(w.offs, w.nbra, t);
         const int j = __ldg(w.kstart + i) + (int)(t - __ldg(w.offs + i));
         const ShellPair P = w.bra[i];
@@ -439,8 +492,8 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
 
 template <int LA, int LB, int LC, int LD>
 void launch_store(const BatchWork& w, const PrimPair* prims, const double* boys, double* out,
-                  unsigned long long* pc, int grid, cudaStream_t s) {
-    qb_batch_store_kernel<LA, LB, LC, LD><<<grid, 128, 0, s>>>(w, prims, boys, out, pc);
+                  unsigned long long* pc, const unsigned* perm, int grid, cudaStream_t s) {
+    qb_batch_store_kernel<LA, LB, LC, LD><<<grid, 128, 0, s>>>(w, prims, boys, out, pc, perm);
 }
 template <int LA, int LB, int LC, int LD>
 void launch_digest(const BatchWork& w, const DigestChunk* chunks, const double* in, const MolDev* mols, int grid,
@@ -450,7 +503,8 @@ void launch_digest(const BatchWork& w, const DigestChunk* chunks, const double* 
 
 struct ClassDef {
     int la, lb, lc, ld, nint;
-    void (*store)(const BatchWork&, const PrimPair*, const double*, double*, unsigned long long*, int, cudaStream_t);
+    void (*store)(const BatchWork&, const PrimPair*, const double*, double*, unsigned long long*, const unsigned*, int,
+                  cudaStream_t);
     void (*digest)(const BatchWork&, const DigestChunk*, const double*, const MolDev*, int, cudaStream_t);
 };
 
@@ -770,6 +824,12 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
                                  s));
     QB_CUDA(ctx, cudaMemsetAsync(d_primcount.p, 0, sizeof(unsigned long long), s));
     BatchWork work[QB_BATCH_NCLASS];
+    long long max_total = 1;
+    for (int c = 0; c < QB_BATCH_NCLASS; ++c) max_total = std::max(max_total, total[c]);
+    if (max_total >= (1LL << 32)) return qb_set_error(ctx, QB_ERR_DIM, "batched SCF: over 2^32 quartets in one class");
+    DevArray<unsigned> d_perm, d_hist;   // visiting order of one class (reused), bucket counters
+    QB_CUDA(ctx, d_perm.ensure((size_t)max_total));
+    QB_CUDA(ctx, d_hist.ensure(QB_COST_BUCKETS));
     for (int c = 0; c < QB_BATCH_NCLASS; ++c) {
         const ClassDef& cd = kClasses[c];
         const int X = pc_of(cd.la, cd.lb), Y = pc_of(cd.lc, cd.ld);
@@ -777,7 +837,11 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
                             pc_off[X + 1] - pc_off[X], X == Y};
         if (total[c] == 0) continue;
         const int grid = (int)std::min<long long>((total[c] + 127) / 128, (long long)ctx->nsm * 16);
-        cd.store(work[c], d_prims.p, ctx->boys.p, d_eri.p + eri_at[c], d_primcount.p, grid, s);
+        QB_CUDA(ctx, cudaMemsetAsync(d_hist.p, 0, QB_COST_BUCKETS * sizeof(unsigned), s));
+        qb_batch_cost_hist_kernel<<<grid, 128, 0, s>>>(work[c], d_hist.p);
+        qb_batch_cost_scan_kernel<<<1, 1, 0, s>>>(d_hist.p);
+        qb_batch_cost_scatter_kernel<<<grid, 128, 0, s>>>(work[c], d_hist.p, d_perm.p);
+        cd.store(work[c], d_prims.p, ctx->boys.p, d_eri.p + eri_at[c], d_primcount.p, d_perm.p, grid, s);
     }
     QB_CUDA(ctx, cudaGetLastError());
     // ---- digest chunks: per class and molecule, runs of at most QB_DIGEST_CHUNK quartets
