@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
     }
     // F' = X^T F X  (W2)
     qb_cta_gemm(false, false, n, n, n, 1.0, M.F, n, M.X, n, 0.0, M.W1, n);
-    qb_cta_gemm(true, false, n, n, n, 1.0, M.X, n, M.W1, n, 0.0, M.W2, n);
+    qb_cta_gemm_sym(true, false, n, n, M.X, n, M.W1, n, M.W2, n);
     if (it > 0 && prm.diis > 1) {
         // DIIS subspace of (F', e', E) entries (initializeHFcore, HartreeFock.jl:1335-1394):
         // the entry of this density joins, then either the subspace restarts from the
@@ -429,9 +429,9 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
         for (int i = tid; i < nn; i += nt) Aw[i] = M.W2[i];
         __syncthreads();
         qb_cta_lowest_eig<QB_BATCH_MAXN>(n, k, Aw, Yw, M.eps, M.W4, M.W5, M.W6, M.wt, esm);
-        qb_cta_gemm(false, true, n, n, k, 1.0, Yw, n, Yw, n, 0.0, M.W3, n);
+        qb_cta_gemm_sym(false, true, n, k, Yw, n, Yw, n, M.W3, n);
         qb_cta_gemm(false, false, n, k, n, 1.0, M.X, n, Yw, n, 0.0, M.W4, n);
-        qb_cta_gemm(false, true, n, n, M.nocc, 1.0, M.W4, n, M.W4, n, 0.0, M.W2, n);
+        qb_cta_gemm_sym(false, true, n, k, M.W4, n, M.W4, n, M.W2, n);
     } else {
         // rotate into the previous eigenvectors, A = C'^T F' C' (W3), and diagonalise;
         // eigenvectors to off(A) <= 1e-12 ||A||: the density they give is exact far below

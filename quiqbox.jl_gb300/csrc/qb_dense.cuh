@@ -53,6 +53,35 @@ static __device__ void qb_cta_gemm(bool tA, bool tB, int m, int n, int k, double
     __syncthreads();
 }
 
+// C = op(A) op(B) (n x n, k inner) for a product known to be symmetric (X^T (F X), Y Y^T,
+// (X Y)(X Y)^T): each entry i <= j is computed once and written to both (i, j) and (j, i).
+// Ends with a block barrier.
+static __device__ void qb_cta_gemm_sym(bool tA, bool tB, int n, int k, const double* A, int lda, const double* B,
+                                       int ldb, double* C, int ldc) {
+    const int npair = n * (n + 1) / 2;
+    for (int idx = threadIdx.x; idx < npair; idx += blockDim.x) {
+        // idx -> (i, j), j >= i, packed column by column (FP32 estimate, exact after the
+        // corrections: 8 idx + 1 < 2^24 for n <= 2048)
+        int j = (int)((sqrtf(8.0f * (float)idx + 1.0f) - 1.0f) * 0.5f);
+        while (j * (j + 1) / 2 > idx) --j;
+        while ((j + 1) * (j + 2) / 2 <= idx) ++j;
+        const int i = idx - j * (j + 1) / 2;
+        double s = 0.0;
+        if (!tA && !tB) {
+            for (int p = 0; p < k; ++p) s = fma(A[i + (size_t)lda * p], B[p + (size_t)ldb * j], s);
+        } else if (tA && !tB) {
+            for (int p = 0; p < k; ++p) s = fma(A[p + (size_t)lda * i], B[p + (size_t)ldb * j], s);
+        } else if (!tA && tB) {
+            for (int p = 0; p < k; ++p) s = fma(A[i + (size_t)lda * p], B[j + (size_t)ldb * p], s);
+        } else {
+            for (int p = 0; p < k; ++p) s = fma(A[p + (size_t)lda * i], B[j + (size_t)ldb * p], s);
+        }
+        C[i + (size_t)ldc * j] = s;
+        C[j + (size_t)ldc * i] = s;
+    }
+    __syncthreads();
+}
+
 // Shared-memory scratch of qb_cta_jacobi for matrices up to MAXN.
 template <int MAXN>
 struct QbJacobiSmem {
