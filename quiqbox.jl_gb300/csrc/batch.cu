@@ -66,7 +66,8 @@ struct DigestChunk {
     int b0, b1;              // bras [b0, b1) own them (offs[b0] <= t0, offs[b1] >= t1)
     int mol, pad;
 };
-#define QB_DIGEST_CHUNK 2048
+#define QB_DIGEST_CHUNK 2048        // quartets per digest block of a molecule with much work in a class
+#define QB_DIGEST_CHUNK_SMALL 512   // ... and of the others (enough blocks to spread a straggler)
 
 struct MolDev {
     int n, nocc, conv, iter;   // conv: 0 iterating, 1 converged, 2 stopped at max_iter, 3 failed
@@ -845,6 +846,8 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     }
     QB_CUDA(ctx, cudaGetLastError());
     // ---- digest chunks: per class and molecule, runs of at most QB_DIGEST_CHUNK quartets
+    // (QB_DIGEST_CHUNK_SMALL for a molecule with fewer than 128 such runs in the class: its
+    // late iterations then still spread over many SMs)
     std::vector<DigestChunk> h_chunks;
     std::vector<size_t> chunk_at(QB_BATCH_NCLASS + 1, 0);
     for (int c = 0; c < QB_BATCH_NCLASS; ++c) {
@@ -854,8 +857,10 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
         const long long* off = h_offs.data() + offs_at[c];
         for (int m = 0; m < nmol; ++m) {
             const int s0 = seg[X][m], s1 = seg[X][m + 1];
-            for (long long t0 = off[s0]; t0 < off[s1]; t0 += QB_DIGEST_CHUNK) {
-                const long long t1 = std::min<long long>(t0 + QB_DIGEST_CHUNK, off[s1]);
+            const long long chunk = (off[s1] - off[s0]) >= 128LL * QB_DIGEST_CHUNK ? QB_DIGEST_CHUNK
+                                                                                   : QB_DIGEST_CHUNK_SMALL;
+            for (long long t0 = off[s0]; t0 < off[s1]; t0 += chunk) {
+                const long long t1 = std::min<long long>(t0 + chunk, off[s1]);
                 // bras owning [t0, t1): largest b with off[b] <= t0, one past the largest with off[b] <= t1 - 1
                 const int b0 = (int)(std::upper_bound(off + s0, off + s1, t0) - off) - 1;
                 const int b1 = (int)(std::upper_bound(off + s0, off + s1, t1 - 1) - off);
