@@ -88,3 +88,33 @@ def test_batch_molecule_generator():
         u, v = P[k - 1] - P[k], P[k + 1] - P[k]
         ang = np.degrees(np.arccos(u @ v / np.linalg.norm(u) / np.linalg.norm(v)))
         assert 95.0 - 1e-9 <= ang <= 130.0 + 1e-9
+
+
+def test_warp_kernel_configs_fit_shared_memory():
+    # every generated warp-kernel configuration (per class: owners G, rows S, warps per
+    # block, cooperative epilogue) must fit a block's 227 KB of shared memory with its
+    # static tables; variant 4 exists for the classes with >= 90 contracted targets
+    import importlib.util
+    from pathlib import Path
+    gen = Path(__file__).resolve().parents[1] / "quiqbox.jl_gb300" / "csrc" / "gen_eri.py"
+    spec = importlib.util.spec_from_file_location("gen_eri", gen)
+    g = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(g)
+    seen4 = 0
+    for cls in g.quartet_classes(2):
+        cg = g.ClassGen(*cls)
+        nt = len(cg.esets) * len(cg.fsets)
+        la, lb, lc, ld = cls
+        nint = g.ncart(la) * g.ncart(lb) * g.ncart(lc) * g.ncart(ld)
+        nab, nf = g.ncart(la) * g.ncart(lb), len(cg.fsets)
+        cfgs = g.warp_configs(nt, nint, nab, nf)
+        for v, (G, S, rg, pl, coop, wpb) in cfgs.items():
+            dyn = wpb * (S * G * (nt | 1) + (nab * nf + nint if coop else 0)) * 8
+            # static tables: counts (2 B x 32 per owner), level table, per-owner ints, window
+            static = wpb * (G * 32 * 2 + 257 * 4 + 5 * G * 4 + G + (128 * 9 if rg else 9))
+            assert dyn + static <= 227 * 1024, (cls, v)
+            assert 1 <= G <= 32 and 1 <= S <= 4
+            assert coop == (v == 4 and nint >= g.COOP_MIN_NINT)
+        assert (4 in cfgs) == (nt >= g.BIG_NT), cls
+        seen4 += 4 in cfgs
+    assert seen4 >= 8
