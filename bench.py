@@ -449,7 +449,7 @@ def batched_rhf(qb, n_mol, seed, cpu_seconds):
         nocc = (int(round(nuc.charges.sum())) - m["charge"]) // 2
         t1 = time.perf_counter()
         ro = oracle.hartree_fock(fb, nuc.charges, nuc.positions, nocc, nocc, guess="CoreH", methods=("DIIS",),
-                                 intervals=(1e-10,), secondary=(1e6, 100.0), max_step=200)
+                                 intervals=(1e-10,), secondary=(1e6, 100.0), max_step=200, solvers=("LCM",))
         t_cpu += time.perf_counter() - t1
         done += 1
         cpu_conv += int(ro["converged"] == 1)

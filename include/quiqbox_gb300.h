@@ -189,8 +189,12 @@ int qb_jk_pair_table(qb_ctx* ctx, int* npair, int* fa, int* fb, int* la, int* lb
 
 /* Hartree–Fock SCF (runHartreeFock, src/HartreeFock.jl:953-1228) on the GPU:
  * symmetric orthogonalisation, Jacobi diagonalisation, direct J/K Fock build,
- * DD / DIIS / EDIIS / ADIIS convergence methods (Lagrange-multiplier solver). */
+ * DD / DIIS / EDIIS / ADIIS convergence methods with the reference's three DIIS
+ * coefficient solvers (constraintSolver!, src/HartreeFock.jl:1479-1487):
+ * QB_DIIS_LBFGS (L-BFGS-B, the default :17), QB_DIIS_SPGB (spectral projected
+ * gradient) and QB_DIIS_LCM (Lagrange multipliers, CMsolver!). */
 enum { QB_SCF_DD = 0, QB_SCF_DIIS = 1, QB_SCF_EDIIS = 2, QB_SCF_ADIIS = 3 };
+enum { QB_DIIS_LBFGS = 0, QB_DIIS_SPGB = 1, QB_DIIS_LCM = 2 };
 enum { QB_GUESS_COREH = 0, QB_GUESS_GWH = 1, QB_GUESS_SAD = 2, QB_GUESS_DIRECT = 3 };
 
 typedef struct {
@@ -207,6 +211,7 @@ typedef struct {
     int diis_size;                /* default 15                                                  */
     double damp_strength;         /* DD damping, default 0.75                                    */
     double schwarz;               /* J/K screening threshold (default 1e-14)                     */
+    int solver[8];                /* per method: QB_DIIS_* coefficient solver (default LBFGS)    */
 } qb_scf_config;
 
 typedef struct {
@@ -273,6 +278,16 @@ typedef struct {
 void qb_batch_config_default(qb_batch_config* cfg);
 int qb_run_rhf_batched(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nnuc, const double* Z,
                        const double* R, const int* nocc, const qb_batch_config* cfg, qb_batch_result* res);
+
+/* One DIIS coefficient solve on the device, the step of xDIIScore! (src/HartreeFock.jl:1322-1331)
+ * that constraintSolver! (:1479-1487) performs: minimise v.c/s + c^T B c/(2 s^2), s = sum c
+ * (genxDIISf, :1398-1404), with c >= 0 when convex != 0 (EDIIS / ADIIS).  B is m x m
+ * column-major, v has m entries (NULL = zeros, as DIIS), 1 <= m <= 15; c (m) is the starting
+ * point on entry (the reference carries the previous solution over) and the normalised
+ * coefficients on return.  solver: QB_DIIS_LBFGS, QB_DIIS_SPGB or QB_DIIS_LCM.  iterations
+ * (may be NULL) receives the L-BFGS-B iteration count. */
+int qb_diis_coefficients(qb_ctx* ctx, int solver, int convex, int m, const double* B, const double* v, double* c,
+                         int* iterations);
 
 /* Measured FP64 FMA throughput of this device (TFLOP/s), the FP64 roofline denominator. */
 int qb_fp64_peak(qb_ctx* ctx, double* tflops);

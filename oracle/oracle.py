@@ -57,7 +57,9 @@ def lib():
         L.qbo_num_threads.restype = _i
         L.qbo_hartree_fock.restype = _i
         L.qbo_hartree_fock.argtypes = basis + [_i, _pd, _pd, _i, _i, _i, _i, C.c_void_p, _i, _pi,
-                                               _pd, _d, _d, _d, _i, _i, _pd, _pd, _pd, _pd, _pd]
+                                               _pd, _pi, _d, _d, _d, _i, _i, _pd, _pd, _pd, _pd, _pd]
+        L.qbo_diis_solve_iter.restype = _i
+        L.qbo_diis_solve_iter.argtypes = [_i, _i, _i, _pd, _pd, _pd]
         L.qbo_eigh.argtypes = [_i, _pd, _pd, _pd]
         _lib = L
     return _lib
@@ -190,12 +192,22 @@ def jk(fb, D, nthreads=0, exact=False):
 
 
 METHODS = {"DD": 0, "DIIS": 1, "EDIIS": 2, "ADIIS": 3}
+SOLVERS = {"LBFGS": 0, "SPGB": 1, "LCM": 2}
+
+
+def diis_solve(solver, convex, v, B, c0):
+    """One DIIS coefficient solve (constraintSolver!, HartreeFock.jl:1479-1487) from the
+    starting point c0; returns (normalised c, iterations or status)."""
+    c = _v(c0).copy()
+    Bf = np.ascontiguousarray(np.asarray(B, np.float64).T)   # column-major
+    it = lib().qbo_diis_solve_iter(SOLVERS[solver], int(convex), len(c), _v(v), Bf.reshape(-1), c)
+    return c, it
 GUESSES = {"CoreH": 0, "GWH": 1, "SAD": 2, "Direct": 3}
 
 
 def hartree_fock(fb, Z, R, nalpha, nbeta, uhf=False, guess="CoreH", C0=None,
                  methods=("DD", "ADIIS", "DIIS"), intervals=(5e-3, 1e-4, 1e-9),
-                 secondary=(1000.0, 1000.0), osc=5e-6, max_step=200, early_stop=True):
+                 secondary=(1000.0, 1000.0), osc=5e-6, max_step=200, early_stop=True, solvers=None):
     n = fb.nfun
     ns = 2 if uhf else 1
     Cout, Dout, Fout = (np.zeros(ns * n * n) for _ in range(3))
@@ -209,7 +221,8 @@ def hartree_fock(fb, Z, R, nalpha, nbeta, uhf=False, guess="CoreH", C0=None,
     st = lib().qbo_hartree_fock(*_b(fb), len(Zc), Zc, Rc, int(nalpha), int(nbeta), int(uhf),
                                 GUESSES[guess], None if c0 is None else c0.ctypes.data,
                                 len(methods), _v([METHODS[m] for m in methods], np.int32),
-                                _v(intervals), float(secondary[0]), float(secondary[1]), float(osc),
+                                _v(intervals), _v([SOLVERS[x] for x in (solvers or ["LBFGS"] * len(methods))], np.int32),
+                                float(secondary[0]), float(secondary[1]), float(osc),
                                 int(max_step), int(early_stop), Cout, Dout, Fout, eps, info)
     if st != 0:
         raise ValueError("oracle Hartree-Fock rejected its arguments")

@@ -8,10 +8,13 @@
 // guesses (:195-293) with breakCoeffSymmetry (:71-140), and runHartreeFockCore
 // (:1049-1228) with the DD (:1245-1270) and DIIS / EDIIS / ADIIS cores
 // (:1273-1394) including subspace reset/eviction.  The DIIS coefficient problem
-// is solved by the reference's Lagrange-multiplier solver CMsolver!
-// (:1445-1477).  The reference's default solver is L-BFGS-B (LBFGSB.jl 0.4.1,
-// Fortran, not vendored); converged energies and densities do not depend on the
-// solver beyond round-off, iteration trajectories do.
+// is solved by the solver each method names (constraintSolver!, :1479-1487):
+// L-BFGS-B (the default, LBFGSBsolver! :1416-1430) or the spectral projected
+// gradient (SPGBsolver! :1432-1443), both restated in oracle_diis.cpp, or the
+// Lagrange-multiplier solver CMsolver! (:1445-1477) restated here.  The
+// coefficient vector of each method persists between its steps, as the
+// reference's `cs` does: the solution of one step, with a 1 appended for the
+// newest entry, starts the next solve.
 //
 // LAPACK's `eigen(Hermitian)` is replaced by a cyclic Jacobi eigensolver
 // (ascending eigenvalues), LU with partial pivoting replaces `\` and `det`.
@@ -32,6 +35,7 @@ void qbo_one_body(int kind, int nfun, const int* fp, const double* cen, const in
                   const double* R, double* out);
 void qbo_eri_tensor(int nfun, const int* fp, const double* cen, const int* ijk,
                     const double* alpha, const double* w, double* eri);
+int qbo_diis_solve_iter(int solver, int convex, int n, const double* v, const double* B, double* c);
 }
 
 namespace {
@@ -459,6 +463,7 @@ bool oscillate_converged(const std::vector<double>& seq, double tar, int minLen,
 // One SCF method core: DD (HartreeFock.jl:1245-1270) or a DIIS variant (:1335-1394)
 struct Core {
     int method;   // 0 DD, 1 DIIS, 2 EDIIS, 3 ADIIS
+    int solver = 0;   // 0 L-BFGS-B (default, HartreeFock.jl:17), 1 SPG, 2 Lagrange multipliers
     double damp = 0.75;
     int diis_size = 15;
     double reset = 1000 * kAtolVal;
@@ -503,7 +508,10 @@ Step run_core(const System& s, Core& core, std::vector<Trace>& t) {
                     B[i + size_t(m) * j] =
                         dotv(s.M.add(Ds[i], Ds[m - 1], -1.0), s.M.add(Fs[j], Fs[m - 1], -1.0));
         }
-        cm_solver(core.method != 1, core.cs[k], v, B);
+        if (core.solver == 2)
+            cm_solver(core.method != 1, core.cs[k], v, B);
+        else
+            qbo_diis_solve_iter(core.solver, core.method != 1, m, v.data(), B.data(), core.cs[k].data());
         Mat F = s.M.zeros();
         for (int i = 0; i < m; ++i) F = s.M.add(F, Fs[i], core.cs[k][i]);
         Fn.push_back(F);
@@ -543,8 +551,8 @@ struct Result {
 
 // runHartreeFockCore (HartreeFock.jl:1049-1228)
 Result scf_core(const System& s, std::vector<Mat> C0, int nmeth, const int* methods,
-                const double* intervals, double ratio1, double ratio2, double oscThr, int maxStep,
-                bool earlyStop, std::vector<Trace>& t, Shared& sh) {
+                const double* intervals, const int* solvers, double ratio1, double ratio2, double oscThr,
+                int maxStep, bool earlyStop, std::vector<Trace>& t, Shared& sh) {
     // initializeSCF (:526-542)
     t.assign(s.nspin, Trace{});
     std::vector<Mat> D;
@@ -570,6 +578,7 @@ Result scf_core(const System& s, std::vector<Mat> C0, int nmeth, const int* meth
         const size_t len = methods[l] == 0 ? 3 : 15;   // max(HFinterMatStoreSizes..., cache size)
         Core core;
         core.method = methods[l];
+        core.solver = solvers ? solvers[l] : 0;
         if (core.method != 0) {   // initializeHFcore for DIIS types (:1335-1360)
             const size_t init = std::min<size_t>(core.diis_size, t[0].Ds.size());
             for (int k = 0; k < s.nspin; ++k) {
@@ -630,7 +639,8 @@ Result scf_core(const System& s, std::vector<Mat> C0, int nmeth, const int* meth
 extern "C" {
 
 // Hartree–Fock on a stored ERI tensor.
-//   methods: 0 DD, 1 DIIS, 2 EDIIS, 3 ADIIS (all with the Lagrange-multiplier solver)
+//   methods: 0 DD, 1 DIIS, 2 EDIIS, 3 ADIIS; solvers (per method, may be null = all
+//            L-BFGS-B): 0 L-BFGS-B, 1 SPG, 2 Lagrange multipliers
 //   guess:   0 CoreH, 1 GWH, 2 SAD, 3 Direct (C0 given, nspin matrices)
 // Outputs (nspin blocks of n*n / n): C, D, F, orbital energies; scalars in info:
 //   info[0] = E_elec, info[1] = converged (0 no, 1 yes, 2 oscillation), info[2] = steps
@@ -638,7 +648,7 @@ int qbo_hartree_fock(int nfun, const int* fp, const double* cen, const int* ijk,
                      const double* alpha, const double* w, int nnuc, const double* Z,
                      const double* R, int nalpha, int nbeta, int uhf, int guess,
                      const double* C0, int nmeth, const int* methods, const double* intervals,
-                     double ratio1, double ratio2, double oscThr, int maxStep, int earlyStop,
+                     const int* solvers, double ratio1, double ratio2, double oscThr, int maxStep, int earlyStop,
                      double* Cout, double* Dout, double* Fout, double* eps, double* info) {
     const int n = nfun;
     if ((!uhf && nalpha != nbeta) || nmeth < 1) return -1;
@@ -688,7 +698,7 @@ int qbo_hartree_fock(int nfun, const int* fp, const double* cen, const int* ijk,
                 Shared sa;
                 const int m3 = 3;
                 const double iv = std::max(1e-2, 10 * kAtolVal);
-                scf_core(a, Ca, 1, &m3, &iv, 1000.0, 1000.0, 5e-6, 50, true, ta, sa);
+                scf_core(a, Ca, 1, &m3, &iv, nullptr, 1000.0, 1000.0, 5e-6, 50, true, ta, sa);
                 Da = s.M.add(Da, ta[0].Ds.back());
                 Db = s.M.add(Db, ta[1].Ds.back());
             }
@@ -723,7 +733,7 @@ int qbo_hartree_fock(int nfun, const int* fp, const double* cen, const int* ijk,
     }
     std::vector<Trace> t;
     Shared sh;
-    const Result r = scf_core(s, Cinit, nmeth, methods, intervals, ratio1, ratio2, oscThr, maxStep,
+    const Result r = scf_core(s, Cinit, nmeth, methods, intervals, solvers, ratio1, ratio2, oscThr, maxStep,
                               earlyStop != 0, t, sh);
     for (int k = 0; k < s.nspin; ++k) {
         std::memcpy(Cout + size_t(k) * n * n, t[k].Cs.back().data(), sizeof(double) * n * n);
@@ -737,6 +747,13 @@ int qbo_hartree_fock(int nfun, const int* fp, const double* cen, const int* ijk,
     info[1] = r.converged;
     info[2] = r.steps;
     return 0;
+}
+
+// CMsolver! (HartreeFock.jl:1445-1477) on its own: c (n) receives the coefficients.
+void qbo_diis_cm(int convex, int n, const double* v, const double* B, double* c) {
+    std::vector<double> cv(c, c + n), vv(v, v + n), Bv(B, B + size_t(n) * n);
+    cm_solver(convex != 0, cv, vv, Bv);
+    std::memcpy(c, cv.data(), sizeof(double) * n);
 }
 
 // Symmetric eigen-decomposition exposed for tests (ascending).

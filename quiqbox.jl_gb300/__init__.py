@@ -13,7 +13,7 @@ from .api import (overlaps, overlap, elecKinetics, elecKinetic, nucAttractions, 
                   coreHamiltonian, elecRepulsions, elecRepulsion, elecRepulsion_list, jk, SCFconfig,
                   HFconfig, HFfinalInfo, runHartreeFock, RCHartreeFock, UOHartreeFock, fp64_peak, device_info,
                   computeBoysSequence, computeBoysFunc, multipoleMoments, multipoleMoment,
-                  runHartreeFockBatched, BatchSCFConfig, BatchSCFResult, jk_autotune,
+                  runHartreeFockBatched, BatchSCFConfig, BatchSCFResult, jk_autotune, diis_coefficients,
                   DimensionMismatch, DomainError)
 from ._lib import Context, load as load_library, LIB_PATH, EXPORTED  # noqa: F401
 from .differentiation import GaussShell, rhf_energy_gradient, rhf_energy  # noqa: F401

@@ -24,7 +24,7 @@ EXPORTED = ["qb_create", "qb_destroy", "qb_last_error", "qb_device_info", "qb_ov
             "qb_batch_config_default", "qb_run_rhf_batched", "qb_jk_autotune",
             "qb_bf16_gemm_nt", "qb_gelu_forward", "qb_gelu_backward", "qb_f32_to_bf16", "qb_bf16_transpose",
             "qb_colsum", "qb_mse_grad", "qb_adam_step", "qb_adjoint_jk", "qb_eigh_lowest",
-            "qb_guess_features", "qb_guess_assemble"]
+            "qb_guess_features", "qb_guess_assemble", "qb_diis_coefficients"]
 
 
 class DimensionMismatch(ValueError):
@@ -55,7 +55,8 @@ class QBSCFConfig(C.Structure):
     _fields_ = [("uhf", C.c_int), ("guess", C.c_int), ("C0", C.POINTER(C.c_double)), ("nmethod", C.c_int),
                 ("method", C.c_int * 8), ("interval", C.c_double * 8), ("secondary_ratio", C.c_double * 2),
                 ("oscillate_threshold", C.c_double), ("max_step", C.c_int), ("early_stop", C.c_int),
-                ("diis_size", C.c_int), ("damp_strength", C.c_double), ("schwarz", C.c_double)]
+                ("diis_size", C.c_int), ("damp_strength", C.c_double), ("schwarz", C.c_double),
+                ("solver", C.c_int * 8)]
 
 
 class QBSCFResult(C.Structure):
@@ -107,6 +108,7 @@ def load():
         L.qb_run_hartree_fock.argtypes = [vp, pb, C.c_int, pd, pd, C.c_int, C.c_int, C.POINTER(QBSCFConfig),
                                           C.POINTER(QBSCFResult)]
         L.qb_fp64_peak.argtypes = [vp, pd]
+        L.qb_diis_coefficients.argtypes = [vp, C.c_int, C.c_int, C.c_int, pd, vp, pd, C.POINTER(C.c_int)]
         L.qb_jk_noalloc.argtypes = [pb, vp, vp, vp, vp]
         for name in EXPORTED:
             f = getattr(L, name)

@@ -166,15 +166,17 @@ def jk(basis, D, schwarz=1e-12, ctx=None):
 RCHartreeFock = "RHF"   # restricted closed-shell (HartreeFock.jl:61)
 UOHartreeFock = "UHF"   # unrestricted open-shell (HartreeFock.jl:62)
 _METHODS = {"DD": 0, "DIIS": 1, "EDIIS": 2, "ADIIS": 3}
+_SOLVERS = {"LBFGS": 0, "SPGB": 1, "LCM": 2}   # ConstraintSolvers (HartreeFock.jl:1480)
 _GUESSES = {"CoreH": 0, "GWH": 1, "SAD": 2, "Direct": 3}
 
 
 @dataclass
 class SCFconfig:
     """SCF strategy (HartreeFock.jl:659-693): methods with their stopping thresholds
-    (the last converges), per-method keywords (DIISsize, dampStrength; the DIIS
-    coefficient problem uses the Lagrange-multiplier solver), secondary
-    convergence ratios and the oscillation threshold."""
+    (the last converges), per-method keywords keyed by the method's 1-based position as
+    the reference's ``Dict(2=>[:solver=>:LCM])`` (``solver``: "LBFGS" (default), "SPGB"
+    or "LCM", HartreeFock.jl:1480; ``DIISsize``; ``dampStrength``), secondary convergence
+    ratios and the oscillation threshold."""
     methods: Sequence[str] = ("DD", "ADIIS", "DIIS")
     intervals: Sequence[float] = (5e-3, 1e-4, 1e-9)
     config: dict = field(default_factory=dict)
@@ -187,6 +189,17 @@ class SCFconfig:
         for m in self.methods:
             if m not in _METHODS:
                 raise ValueError(f"unknown SCF method {m}")
+        for idx, kws in self.config.items():
+            if not 1 <= int(idx) <= len(self.methods):
+                raise ValueError(f"method index {idx} out of range")
+            for key, val in dict(kws).items():
+                if key == "solver" and val not in _SOLVERS:
+                    # getproperty(ConstraintSolvers, solver) (HartreeFock.jl:1482-1487) has no such field
+                    raise ValueError(f"unknown DIIS solver {val!r} (LBFGS, SPGB or LCM)")
+
+    def solver_of(self, k: int) -> str:
+        """The coefficient solver of method k (0-based)."""
+        return dict(self.config.get(k + 1, {})).get("solver", "LBFGS")
         if np.ndim(self.secondaryConvRatio) == 0:
             self.secondaryConvRatio = (float(self.secondaryConvRatio),) * 2
 
@@ -262,6 +275,7 @@ def runHartreeFock(nucInfo, basis, config: Optional[HFconfig] = None, spin=None,
     for k, (m, iv) in enumerate(zip(st.methods, st.intervals)):
         cfg.method[k] = _METHODS[m]
         cfg.interval[k] = float(iv)
+        cfg.solver[k] = _SOLVERS[st.solver_of(k)]
     kw = {}
     for d in st.config.values():
         kw.update(dict(d))
@@ -295,6 +309,28 @@ def runHartreeFock(nucInfo, basis, config: Optional[HFconfig] = None, spin=None,
     conv = {0: False, 1: True, 2: True}[res.converged]
     return HFfinalInfo((res.E_elec, nucRepulsion(nucInfo)), mats(Cb), mats(Db), mats(Fb), tuple(occ), conv,
                        res.steps, (na, nb))
+
+
+def diis_coefficients(B, v=None, c0=None, solver="LBFGS", convex=False, ctx=None):
+    """One DIIS coefficient solve on the device (constraintSolver!, HartreeFock.jl:1479-1487):
+    minimise v.c/s + c^T B c/(2 s^2), s = sum(c), with c >= 0 when ``convex`` (EDIIS /
+    ADIIS).  ``c0`` is the starting point (default 1, 2, ..., m, as a new subspace starts).
+    Returns (normalised c, solver iterations)."""
+    if solver not in _SOLVERS:
+        raise ValueError(f"unknown DIIS solver {solver!r} (LBFGS, SPGB or LCM)")
+    Bm = np.asarray(B, np.float64)
+    m = Bm.shape[0]
+    if Bm.shape != (m, m):
+        raise DimensionMismatch("B must be square")
+    Bf = np.ascontiguousarray(Bm.reshape(-1, order="F"))
+    vv = None if v is None else np.ascontiguousarray(np.asarray(v, np.float64).reshape(m))
+    c = np.ascontiguousarray(np.arange(1.0, m + 1) if c0 is None else np.asarray(c0, np.float64).reshape(m)).copy()
+    it = C.c_int(0)
+    cx = _ctx(ctx)
+    cx.check(cx.lib.qb_diis_coefficients(cx.h, _SOLVERS[solver], int(bool(convex)), m, L.dptr(Bf),
+                                         None if vv is None else vv.ctypes.data_as(C.c_void_p), L.dptr(c),
+                                         C.byref(it)))
+    return c, it.value
 
 
 def jk_autotune(basis, D, schwarz=1e-12, repeats=1, ctx=None):

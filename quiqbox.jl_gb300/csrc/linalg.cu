@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include "qb_internal.h"
 #include "qb_dense.cuh"
+#include "qb_diis_solvers.cuh"
 
 // ---------------------------------------------------------------------------
 // C = alpha op(A) op(B) + beta C, column-major, 32x32 tiles in shared memory,
@@ -324,10 +325,20 @@ __global__ void qb_diis_kernel(int m, int convex, const double* Bin, const doubl
     atomicOr(status, 4);
 }
 
-int qb_diis_solve(cudaStream_t s, int m, int convex, const double* B, const double* v, double* c, double* work,
-                  int* status) {
-    (void)work;
+// L-BFGS-B / SPG solve by one thread (qb_diis_solvers.cuh); c holds the starting point.
+__global__ void qb_diis_iter_kernel(int solver, int convex, int m, const double* B, const double* v, double* c,
+                                    QbDiisWork* work) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) qb_diis_iterative_solve(*work, solver, convex, m, B, m, v, c);
+}
+
+int qb_diis_solve(cudaStream_t s, int m, int convex, int solver, const double* B, const double* v, double* c,
+                  QbDiisWork* work, int* status) {
     if (m < 1 || m > QB_DIIS_MAX) return -1;
-    qb_diis_kernel<<<1, 32, 0, s>>>(m, convex, B, v, c, status);
+    if (solver == QB_DIIS_LCM) {
+        qb_diis_kernel<<<1, 32, 0, s>>>(m, convex, B, v, c, status);
+    } else {
+        if (!work || m > QB_DS_N) return -1;
+        qb_diis_iter_kernel<<<1, 32, 0, s>>>(solver, convex, m, B, v, c, work);
+    }
     return 0;
 }

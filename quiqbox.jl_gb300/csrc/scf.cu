@@ -4,7 +4,9 @@
 // symmetric orthogonalisation X = S^-1/2 (:39-42), Fock diagonalisation with
 // the sign convention of solveFockMatrix (:46-56), getD / getE (:296-342),
 // getCDFE (:392-403), the DD core (:1245-1270) and the DIIS / EDIIS / ADIIS
-// cores (:1273-1394) with subspace reset and eviction, the CoreH / GWH / SAD /
+// cores (:1273-1394) with subspace reset and eviction and the per-method DIIS
+// coefficient solver (L-BFGS-B by default, SPG or Lagrange multipliers, solved on the
+// device, the coefficient vector carried between steps as the reference's `cs`), the CoreH / GWH / SAD /
 // Direct guesses (:195-293) with breakCoeffSymmetry (:71-140), and the
 // convergence, oscillation and early-stop rules (:1142-1203).  Every matrix
 // operation runs as a CUDA kernel of this library; the two-electron part is the
@@ -20,6 +22,7 @@
 #include <string>
 #include <vector>
 #include "qb_internal.h"
+#include "qb_diis_solvers.cuh"
 
 #define QB_TRY(expr)                  \
     do {                              \
@@ -146,6 +149,7 @@ struct Scf {
            *E_d = nullptr;
     const double** ptrs_d = nullptr;
     const double** ptrs2_d = nullptr;
+    QbDiisWork* dwork = nullptr;   // state of the iterative DIIS coefficient solvers
     std::vector<std::unique_ptr<double, void (*)(void*)>> owned;
 
     double* alloc(size_t count) {
@@ -173,6 +177,11 @@ struct Scf {
         owned.emplace_back((double*)p2, [](void* q) { cudaFree(q); });
         ptrs_d = (const double**)p1;
         ptrs2_d = (const double**)p2;
+        void* p3 = nullptr;
+        if (cudaMalloc(&p3, sizeof(QbDiisWork)) != cudaSuccess)
+            return qb_set_error(ctx, QB_ERR_NOMEM, "DIIS solver workspace");
+        owned.emplace_back((double*)p3, [](void* q) { cudaFree(q); });
+        dwork = (QbDiisWork*)p3;
         if (!S || !H || !X || !t1 || !t2 || !t3 || !J || !K || !eigw || !eigwork || !scal || !gram || !B || !v ||
             !c || !E_d)
             return qb_set_error(ctx, QB_ERR_NOMEM, "SCF device buffers");
@@ -373,10 +382,12 @@ bool oscillate_converged(const std::vector<double>& seq, double tar, int minLen,
 
 struct Core {
     int method;
+    int solver = QB_DIIS_LBFGS;   // coefficient solver (defaultDIISsolver, :17)
     double damp = 0.75;
     int diis_size = 15;
     double reset = 1000 * kAtolVal;
     std::vector<std::vector<DiisItem>> sub;   // per spin
+    std::vector<std::vector<double>> cs;      // per spin: coefficient vector, starting point of the next solve
 };
 
 void drop_item(Scf& sc, DiisItem& it) {
@@ -433,15 +444,19 @@ int run_core(Scf& sc, Core& core, RunState& st, StepOut& out) {
         QB_CUDA(sc.ctx, cudaMemcpyAsync(sc.ptrs_d, P.data(), m * sizeof(double*), cudaMemcpyHostToDevice, sc.s));
         QB_CUDA(sc.ctx, cudaMemcpyAsync(sc.ptrs2_d, Q.data(), m * sizeof(double*), cudaMemcpyHostToDevice, sc.s));
         QB_CUDA(sc.ctx, cudaMemcpyAsync(sc.E_d, E.data(), m * sizeof(double), cudaMemcpyHostToDevice, sc.s));
+        QB_CUDA(sc.ctx, cudaMemcpyAsync(sc.c, core.cs[k].data(), m * sizeof(double), cudaMemcpyHostToDevice, sc.s));
         gram_kernel<<<dim3(m, m), 256, 0, sc.s>>>(m, (long long)sc.nn, sc.ptrs_d, sc.ptrs2_d, sc.gram);
         diis_system_kernel<<<1, dim3(16, 16), 0, sc.s>>>(m, core.method, sc.gram, sc.E_d, sc.B, sc.v);
-        qb_diis_solve(sc.s, m, core.method != QB_SCF_DIIS, sc.B, sc.v, sc.c, nullptr, sc.ctx->status.p);
+        if (qb_diis_solve(sc.s, m, core.method != QB_SCF_DIIS, core.solver, sc.B, sc.v, sc.c, sc.dwork,
+                          sc.ctx->status.p) != 0)
+            return qb_set_error(sc.ctx, QB_ERR_ARG, "DIIS subspace size or solver out of range");
         std::vector<const double*> Fp(m);
         for (int i = 0; i < m; ++i) Fp[i] = sub[i].F;
         QB_CUDA(sc.ctx, cudaMemcpyAsync(sc.ptrs_d, Fp.data(), m * sizeof(double*), cudaMemcpyHostToDevice, sc.s));
         Fn[k] = sc.mat();
         if (!Fn[k]) return qb_set_error(sc.ctx, QB_ERR_NOMEM, "SCF matrices");
         qb_lincomb(sc.s, (long long)sc.nn, m, sc.ptrs_d, sc.c, Fn[k]);
+        QB_CUDA(sc.ctx, cudaMemcpyAsync(core.cs[k].data(), sc.c, m * sizeof(double), cudaMemcpyDeviceToHost, sc.s));
         // the pointer table is reused by the next sector: finish this one first
         QB_CUDA(sc.ctx, cudaStreamSynchronize(sc.s));
     }
@@ -449,19 +464,23 @@ int run_core(Scf& sc, Core& core, RunState& st, StepOut& out) {
     for (int k = 0; k < sc.nspin; ++k) sc.drop(Fn[k]);
     for (int k = 0; k < sc.nspin; ++k) {
         auto& sub = core.sub[k];
+        auto& c = core.cs[k];
         QB_TRY(add_item(sc, core, k, out.e[k].D, out.e[k].F, out.e[k].E));
+        c.push_back(1.0);
         const size_t L = sub.size();
         if (L > 2 && sub[L - 1].E - sub[L - 2].E > core.reset) {   // keepOnly! of the second-to-last
             DiisItem keep = sub[L - 2];
             for (size_t i = 0; i < L; ++i)
                 if (i != L - 2) drop_item(sc, sub[i]);
             sub.assign(1, keep);
+            c.assign(1, c[L - 2]);
         } else if ((int)L > core.diis_size) {
             size_t pi = 0;
             for (size_t i = 1; i < L; ++i)
                 if (sub[i].E > sub[pi].E) pi = i;
             drop_item(sc, sub[pi]);
             sub.erase(sub.begin() + pi);
+            c.erase(c.begin() + pi);
         }
     }
     return qb_check_status(sc.ctx);
@@ -475,7 +494,7 @@ struct CoreResult {
 
 // runHartreeFockCore (HartreeFock.jl:1049-1228)
 int scf_core(Scf& sc, double* const* C0, const qb_scf_config& cfg, const int* methods, const double* intervals,
-             int nmeth, int maxStep, RunState& st, CoreResult& res) {
+             const int* solvers, int nmeth, int maxStep, RunState& st, CoreResult& res) {
     st.t.assign(sc.nspin, Trace{});
     {   // initializeSCF (:526-542)
         StepOut r;
@@ -519,10 +538,13 @@ int scf_core(Scf& sc, double* const* C0, const qb_scf_config& cfg, const int* me
         core.method = methods[l];
         core.damp = cfg.damp_strength;
         core.diis_size = cfg.diis_size;
+        core.solver = solvers[l];
         if (core.method != QB_SCF_DD) {   // initializeHFcore for DIIS types (:1335-1360)
             core.sub.resize(sc.nspin);
+            core.cs.resize(sc.nspin);
             const size_t init = std::min<size_t>(core.diis_size, st.t[0].steps.size());
             for (int k = 0; k < sc.nspin; ++k) {
+                for (size_t x = 0; x < init; ++x) core.cs[k].push_back((double)(x + 1));   // collect(OneTo(init))
                 auto& q = st.t[k].steps;
                 for (size_t x = q.size() - init; x < q.size(); ++x) QB_TRY(add_item(sc, core, k, q[x].D, q[x].F, q[x].E));
             }
@@ -621,6 +643,43 @@ extern "C" void qb_scf_config_default(qb_scf_config* cfg) {
     cfg->diis_size = 15;
     cfg->damp_strength = 0.75;
     cfg->schwarz = 1e-14;
+    for (int l = 0; l < 8; ++l) cfg->solver[l] = QB_DIIS_LBFGS;   // defaultDIISsolver (:17)
+}
+
+extern "C" int qb_diis_coefficients(qb_ctx* ctx, int solver, int convex, int m, const double* B, const double* v,
+                                    double* c, int* iterations) {
+    if (!ctx || !B || !c) return qb_set_error(ctx, QB_ERR_ARG, "null argument");
+    if (m < 1 || m > 15) return qb_set_error(ctx, QB_ERR_DOMAIN, "DIIS subspace size must be 1..15");
+    if (solver < QB_DIIS_LBFGS || solver > QB_DIIS_LCM) return qb_set_error(ctx, QB_ERR_ARG, "unknown solver");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return qb_set_error(ctx, QB_ERR_CUDA, "cudaSetDevice");
+    cudaStream_t s = ctx->stream;
+    const size_t bytes = (size_t)m * m * sizeof(double) + 2 * (size_t)m * sizeof(double);
+    double* buf = nullptr;
+    QbDiisWork* w = nullptr;
+    if (cudaMalloc(&buf, bytes) != cudaSuccess) return qb_set_error(ctx, QB_ERR_NOMEM, "DIIS buffers");
+    if (cudaMalloc(&w, sizeof(QbDiisWork)) != cudaSuccess) {
+        cudaFree(buf);
+        return qb_set_error(ctx, QB_ERR_NOMEM, "DIIS solver workspace");
+    }
+    double *dB = buf, *dv = buf + (size_t)m * m, *dc = dv + m;
+    std::vector<double> vz(m, 0.0);
+    int rc = QB_OK;
+    rc = qb_cuda_check(ctx, cudaMemcpyAsync(dB, B, (size_t)m * m * sizeof(double), cudaMemcpyHostToDevice, s), "B");
+    if (rc == QB_OK)
+        rc = qb_cuda_check(ctx, cudaMemcpyAsync(dv, v ? v : vz.data(), m * sizeof(double), cudaMemcpyHostToDevice, s), "v");
+    if (rc == QB_OK) rc = qb_cuda_check(ctx, cudaMemcpyAsync(dc, c, m * sizeof(double), cudaMemcpyHostToDevice, s), "c");
+    if (rc == QB_OK && qb_diis_solve(s, m, convex != 0, solver, dB, dv, dc, w, ctx->status.p) != 0)
+        rc = qb_set_error(ctx, QB_ERR_ARG, "DIIS solve");
+    if (rc == QB_OK) rc = qb_cuda_check(ctx, cudaMemcpyAsync(c, dc, m * sizeof(double), cudaMemcpyDeviceToHost, s), "c");
+    int it = 0;
+    if (rc == QB_OK && iterations)
+        rc = qb_cuda_check(ctx, cudaMemcpyAsync(&it, &w->iters, sizeof(int), cudaMemcpyDeviceToHost, s), "iters");
+    if (rc == QB_OK) rc = qb_cuda_check(ctx, cudaStreamSynchronize(s), "DIIS solve");
+    cudaFree(buf);
+    cudaFree(w);
+    if (rc != QB_OK) return rc;
+    if (iterations) *iterations = solver == QB_DIIS_LCM ? 0 : it;
+    return qb_check_status(ctx);
 }
 
 extern "C" int qb_run_hartree_fock(qb_ctx* ctx, const qb_basis* basis, int nnuc, const double* Z, const double* R,
@@ -633,6 +692,9 @@ extern "C" int qb_run_hartree_fock(qb_ctx* ctx, const qb_basis* basis, int nnuc,
     for (int l = 0; l < cfg->nmethod; ++l)
         if (cfg->method[l] < 0 || cfg->method[l] > 3 || !(cfg->interval[l] >= 0.0) && !std::isnan(cfg->interval[l]))
             return qb_set_error(ctx, QB_ERR_ARG, "bad SCF method or threshold");
+    for (int l = 0; l < cfg->nmethod; ++l)
+        if (cfg->solver[l] < QB_DIIS_LBFGS || cfg->solver[l] > QB_DIIS_LCM)
+            return qb_set_error(ctx, QB_ERR_ARG, "unknown DIIS coefficient solver");
     if (cfg->diis_size < 2 || cfg->diis_size > 15) return qb_set_error(ctx, QB_ERR_DOMAIN, "DIISsize must be 2..15");
     if (!(cfg->damp_strength >= 0.0 && cfg->damp_strength <= 1.0))
         return qb_set_error(ctx, QB_ERR_DOMAIN, "dampStrength must be in [0, 1]");
@@ -724,14 +786,14 @@ extern "C" int qb_run_hartree_fock(qb_ctx* ctx, const qb_basis* basis, int nnuc,
             sc.drop(Cg);
             RunState st;
             CoreResult cr;
-            const int m3 = QB_SCF_ADIIS;
+            const int m3 = QB_SCF_ADIIS, sv = QB_DIIS_LBFGS;   // getDefaultSCFconfigForSAD (:262-264)
             const double iv = std::max(1e-2, 10 * kAtolVal);
             qb_scf_config acfg = *cfg;
             acfg.secondary_ratio[0] = acfg.secondary_ratio[1] = 1000.0;
             acfg.oscillate_threshold = 5e-6;
             acfg.early_stop = 1;
             acfg.diis_size = 15;
-            QB_TRY(scf_core(sc, Ca, acfg, &m3, &iv, 1, 50, st, cr));
+            QB_TRY(scf_core(sc, Ca, acfg, &m3, &iv, &sv, 1, 50, st, cr));
             qb_axpby(s, sc.nn, 1.0, Da, 1.0, st.t[0].steps.back().D, Da);
             qb_axpby(s, sc.nn, 1.0, Db, 1.0, st.t[1].steps.back().D, Db);
             release_state(sc, st);
@@ -786,7 +848,7 @@ extern "C" int qb_run_hartree_fock(qb_ctx* ctx, const qb_basis* basis, int nnuc,
 
     RunState st;
     CoreResult cr;
-    QB_TRY(scf_core(sc, C0, *cfg, cfg->method, cfg->interval, cfg->nmethod, cfg->max_step, st, cr));
+    QB_TRY(scf_core(sc, C0, *cfg, cfg->method, cfg->interval, cfg->solver, cfg->nmethod, cfg->max_step, st, cr));
     // results (HFfinalInfo, :803-819)
     res->E_elec = st.Etots.back();
     double enn = 0.0;   // nucRepulsion (src/Particles.jl:197-210)

@@ -72,11 +72,12 @@ class GradientResult:
 
 
 def tight_scf(conv=1e-12):
-    """CoreH guess, DIIS, |dE| <= conv and RMS(dD) <= 100 conv: tight enough that the
-    energy is stationary to ~conv^2 (what the adjoint formula assumes)."""
+    """CoreH guess, DIIS with the exact (Lagrange-multiplier) coefficients, |dE| <= conv and
+    RMS(dD) <= 100 conv: tight enough that the energy is stationary to ~conv^2 (what the
+    adjoint formula assumes)."""
     from . import api
-    return api.HFconfig(initial="CoreH", strategy=api.SCFconfig(("DIIS",), (conv,), secondaryConvRatio=(1e6, 100.0)),
-                        maxStep=500)
+    return api.HFconfig(initial="CoreH", strategy=api.SCFconfig(("DIIS",), (conv,), {1: [("solver", "LCM")]},
+                                                                secondaryConvRatio=(1e6, 100.0)), maxStep=500)
 
 
 def rhf_energy(nuc, shells, ctx=None, conv=1e-12):

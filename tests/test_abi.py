@@ -39,6 +39,19 @@ def test_default_scf_config_matches_reference(qb):
     assert tuple(cfg.secondary_ratio) == (1000.0, 1000.0)
     assert cfg.oscillate_threshold == 5e-6 and cfg.max_step == 200 and cfg.diis_size == 15
     assert cfg.damp_strength == 0.75 and cfg.guess == 2
+    # defaultDIISsolver = :LBFGS (HartreeFock.jl:17) for every method
+    assert list(cfg.solver) == [0] * 8
+
+
+def test_scfconfig_solver_keywords(qb):
+    # SCFconfig(methods, intervals, Dict(2=>[:solver=>:LCM])) (HartreeFock.jl:645-648, 1480)
+    sc = qb.SCFconfig(("ADIIS", "DIIS", "EDIIS", "DD"), (1e-4, 1e-8, 1e-10, 1e-15),
+                      {1: [("solver", "LCM")], 3: [("solver", "SPGB")]})
+    assert [sc.solver_of(k) for k in range(4)] == ["LCM", "LBFGS", "SPGB", "LBFGS"]
+    with pytest.raises(ValueError):
+        qb.SCFconfig(("DIIS",), (1e-8,), {1: [("solver", "BFGS")]})
+    with pytest.raises(ValueError):
+        qb.SCFconfig(("DIIS",), (1e-8,), {2: [("solver", "LCM")]})
 
 
 def test_null_arguments_are_rejected_without_device(qb):

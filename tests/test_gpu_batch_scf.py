@@ -7,10 +7,12 @@ pytestmark = pytest.mark.gpu
 
 
 def _oracle_rhf(oracle, mol, max_step=300):
+    # the batched path extrapolates with the exact Pulay coefficients, the solution the
+    # Lagrange-multiplier solver gives (CMsolver!, HartreeFock.jl:1445-1477)
     fb, nuc = mol["flat"], mol["nuc"]
     nocc = (int(round(nuc.charges.sum())) - mol["charge"]) // 2
     return oracle.hartree_fock(fb, nuc.charges, nuc.positions, nocc, nocc, guess="CoreH", methods=("DIIS",),
-                               intervals=(1e-10,), secondary=(1e6, 100.0), max_step=max_step)
+                               intervals=(1e-10,), secondary=(1e6, 100.0), max_step=max_step, solvers=("LCM",))
 
 
 def test_batched_rhf_vs_oracle(qb, oracle):
@@ -31,8 +33,8 @@ def test_batched_rhf_matches_single_molecule_path(qb):
     from quiqbox_gb300.workloads import batch_molecules
     mols = [m for m in batch_molecules(12, seed=5, atoms=(2, 8)) if m["charge"] == 0][:6]
     res = qb.runHartreeFockBatched([(m["nuc"], m["flat"]) for m in mols])
-    cfg = qb.HFconfig(initial="CoreH", strategy=qb.SCFconfig(("DIIS",), (1e-10,), secondaryConvRatio=(1e6, 100.0)),
-                      maxStep=300)
+    cfg = qb.HFconfig(initial="CoreH", strategy=qb.SCFconfig(("DIIS",), (1e-10,), {1: [("solver", "LCM")]},
+                                                             secondaryConvRatio=(1e6, 100.0)), maxStep=300)
     for k, m in enumerate(mols):
         r = qb.runHartreeFock(m["nuc"], m["flat"], cfg)
         assert r.converged

@@ -64,7 +64,8 @@ def test_gradient_vs_oracle_finite_differences(qb, oracle):
 
     def e_oracle(sh):
         r = oracle.hartree_fock(shells_basis(sh), nuc.charges, nuc.positions, nocc, nocc, guess="CoreH",
-                                methods=("DIIS",), intervals=(1e-12,), secondary=(1e6, 100.0), max_step=500)
+                                methods=("DIIS",), intervals=(1e-12,), secondary=(1e6, 100.0), max_step=500,
+                                solvers=("LCM",))
         assert r["converged"] == 1
         return r["E_elec"] + qb.nucRepulsion(nuc)
 

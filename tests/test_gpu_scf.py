@@ -29,11 +29,18 @@ def test_h2o_rhf_golden(qb, goldens):
 
 
 def test_h2o_uhf_golden(qb, goldens):
+    # HartreeFock-test.jl:33,37 (SCFc2: LCM for methods 1-3), :152 golden; res2_2 with the
+    # default solvers agrees to 100 x 7.5e-8 (:64)
     h, fb, nuc = _h2o_test(qb, goldens)
+    lcm = {1: [("solver", "LCM")], 2: [("solver", "LCM")], 3: [("solver", "LCM")]}
     cfg = qb.HFconfig(type=qb.UOHartreeFock, initial="GWH",
-                      strategy=qb.SCFconfig(("ADIIS", "DIIS", "EDIIS", "DD"), (1e-4, 1e-8, 1e-10, 1e-15)))
+                      strategy=qb.SCFconfig(("ADIIS", "DIIS", "EDIIS", "DD"), (1e-4, 1e-8, 1e-10, 1e-15), lcm))
     r = qb.runHartreeFock(nuc, fb, cfg)
     assert abs(r.energy[0] - h["uhf_E_elec"]) < 1e-10
+    cfg2 = qb.HFconfig(type=qb.UOHartreeFock, initial="GWH",
+                       strategy=qb.SCFconfig(("ADIIS", "DIIS", "EDIIS", "DD"), (1e-4, 1e-8, 1e-10, 1e-15)))
+    r2 = qb.runHartreeFock(nuc, fb, cfg2)
+    assert abs(r2.energy[0] - r.energy[0]) < 7.5e-6
 
 
 def test_bench_geometry_rhf_vs_oracle(qb, oracle):
@@ -50,8 +57,10 @@ def test_bench_geometry_rhf_vs_oracle(qb, oracle):
 
 @pytest.mark.parametrize("guess", ["CoreH", "SAD"])
 def test_h2_321g_curve_points(qb, goldens, guess):
+    # HartreeFock-test.jl:221-289: all 100 bond lengths, RHF and UHF, default SCFconfig and
+    # solver, maxStep 300, |E - ref| < 10 x 7.5e-8
     hf = goldens["hartree_fock"]
-    for n in (0, 3, 6, 10, 20, 40, 70, 99):
+    for n in range(100):
         L = 0.1 + 0.2 * n
         coords = [(0.0, 0.0, 0.0), (L, 0.0, 0.0)]
         bs = qb.genGaussTypeOrbSeq(coords[0], "H", "3-21G") + qb.genGaussTypeOrbSeq(coords[1], "H", "3-21G")
@@ -61,17 +70,43 @@ def test_h2_321g_curve_points(qb, goldens, guess):
             assert abs(sum(r.energy) - ref[n]) < hf["h2_curve"]["tol"], (L, typ)
 
 
-def test_h2o2_631g_sad(qb, goldens):
+def test_h2o2_631g_all_configs(qb, oracle, goldens):
+    # HartreeFock-test.jl:293-353: the 13 HFconfig cases, default L-BFGS-B solver; 11 reach
+    # the golden (|dE| < 5 x 5e-10, converged); HFc3 / HFc12 (GWH + ADIIS) reach the state
+    # the oracle and an independent restatement reach (tests/test_oracle_goldens.py)
+    from test_oracle_goldens import H2O2_GWH_ADIIS, h2o2_cases, h2o2_system
     h = goldens["hartree_fock"]["h2o2"]
-    coords = [[c * h["angstrom_to_bohr"] for c in x] for x in h["coords_angstrom"]]
-    bs = []
-    for a, x in zip(h["atoms"], coords):
-        bs += qb.genGaussTypeOrbSeq(x, a, "6-31G")
-    nuc = qb.NuclearCluster(h["atoms"], coords)
-    cfg = qb.HFconfig(strategy=qb.SCFconfig.default(threshold=h["threshold"], secondaryConvRatio=(5.0, 5.0)))
-    r = qb.runHartreeFock(nuc, bs, cfg)
-    assert r.converged
-    assert abs(r.energy[0] - h["E_elec"]) < h["tol"]
+    fb, nuc = h2o2_system(qb, h)
+    for name, guess, ms, iv, sec in h2o2_cases(h):
+        cfg = qb.HFconfig(initial=guess, strategy=qb.SCFconfig(ms, iv, secondaryConvRatio=sec), maxStep=200)
+        r = qb.runHartreeFock(nuc, fb, cfg)
+        assert r.converged, name
+        if name in H2O2_GWH_ADIIS:
+            ro = oracle.hartree_fock(fb, nuc.charges, nuc.positions, 9, 9, guess=guess, methods=ms, intervals=iv,
+                                     secondary=sec, max_step=200)
+            assert abs(r.energy[0] - ro["E_elec"]) < h["tol"], name
+        else:
+            assert abs(r.energy[0] - h["E_elec"]) < h["tol"], (name, r.energy[0] - h["E_elec"])
+
+
+def test_device_diis_solvers_match_oracle(qb, oracle):
+    # One coefficient solve (constraintSolver!, HartreeFock.jl:1479-1487) on the device against
+    # the oracle's restatement of the same solver, from the same starting point.
+    rng = np.random.default_rng(11)
+    for m in (1, 2, 3, 6, 10, 15):
+        A = rng.normal(size=(m, 2 * m))
+        for convex in (False, True):
+            B = A @ A.T / m + (0.3 * np.eye(m) if not convex else rng.normal(size=(m, m)))
+            v = np.zeros(m) if not convex else rng.normal(size=m)
+            c0 = rng.uniform(0.1, 1.0, m)
+            for solver in ("LBFGS", "SPGB", "LCM"):
+                cg, itg = qb.diis_coefficients(B, v, c0, solver=solver, convex=convex)
+                co, ito = oracle.diis_solve(solver, convex, v, B, c0)
+                f = lambda c: v @ c + c @ B @ c / 2
+                assert abs(cg.sum() - 1) < 1e-12
+                assert abs(f(cg) - f(co)) < 1e-9 * max(1.0, abs(f(co))), (m, convex, solver)
+                if solver == "LBFGS":
+                    assert np.abs(cg - co).max() < 1e-6, (m, convex, cg, co)
 
 
 def test_dimension_mismatch_of_direct_guess(qb, goldens):
