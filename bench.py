@@ -33,6 +33,13 @@ sys.path.insert(0, str(ROOT / "oracle"))
 METRIC = "ERI GQuartet/s (fused J+K build)"
 UNIT = "GQuartet/s"
 WORKLOAD = "ERI+J/K: 64 H + 16 C/N/O in a 14 bohr cube, 3-prim Cartesian s/p/d shells, N=416, FP64, Schwarz 1e-12"
+L2_NOTE = ("GPU arm: 256 MiB written before every timed build (L2 flush); "
+           "CPU arm: no flush (host caches)")
+
+
+def common_config(nfun, schwarz, quartets):
+    """The `config` both arms print (identical keys and values for the same workload)."""
+    return {"workload": WORKLOAD, "nfun": int(nfun), "schwarz": schwarz, "quartets": int(quartets), "l2": L2_NOTE}
 
 
 def parse():
@@ -278,13 +285,15 @@ def run_reference(args):
         ests.append(last["est_build_s"])
     wall = time.perf_counter() - t0
     value = float(np.mean(vals))
+    # a step is one bounded sample of the build; ms_per_step is its measured wall time, the
+    # full build's extrapolated time is reported separately
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(ests)),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded generator; no dataset)",
-            "config": {"workload": WORKLOAD, "nfun": fb.nfun, "schwarz": args.schwarz,
-                       "quartets": last["quartets"], "parallelism": "host threads (OpenMP)",
-                       "l2": "n/a (CPU)"},
+            "config": common_config(fb.nfun, args.schwarz, last["quartets"]),
+            "details": {"parallelism": "host threads (OpenMP)", "step": "stratified sample of the surviving quartets",
+                        "est_full_build_ms": 1e3 * float(np.mean(ests))},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": last["cores"], "kind": "port",
                              "sample": last["sample"] + f"; {args.steps} sampled steps in {wall:.1f} s wall"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -372,14 +381,13 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded generator; no dataset)",
-            "config": {"workload": WORKLOAD, "nfun": n, "nshell": stats.nshell, "npair": stats.npair,
-                       "schwarz": args.schwarz, "quartets": q, "prim_quartets": int(stats.prim_quartets),
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "l2": "flushed (256 MiB write) before every timed step",
-                       "wall_s_timed_region": wall, "jk_symmetry_rel": sym,
-                       "autotune_s": t_tune,
-                       "kernel_variants": {"".join(str(v) for v in stats.class_l[c]): int(chosen[c])
-                                           for c in range(stats.nclass)}},
+            "config": common_config(n, args.schwarz, q),
+            "details": {"nshell": stats.nshell, "npair": stats.npair, "prim_quartets": int(stats.prim_quartets),
+                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                        "wall_s_timed_region": wall, "jk_symmetry_rel": sym,
+                        "autotune_s": t_tune,
+                        "kernel_variants": {"".join(str(v) for v in stats.class_l[c]): int(chosen[c])
+                                            for c in range(stats.nclass)}},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": None,
                          "peak_source": "measured: FP64 FMA microbenchmark (qb_fp64_peak) in this run",
@@ -399,6 +407,8 @@ def run_ours(args):
         pairs = (arr[0], arr[1], arr[2], arr[3], Qv)
         line["cpu_baseline"] = cpu_baseline(oracle, fb, D, pairs, args.schwarz, args.cpu_seconds)
         line["cpu_baseline"].pop("quartets", None)
+        line["reduced_workload"] = reduced_anchor(qb, ctx, oracle, args.schwarz)
+        line["config0_rhf"] = config0(qb, oracle)
         if args.batch_mols > 0:
             line["batched_rhf"] = batched_rhf(qb, args.batch_mols, args.seed, args.batch_cpu_seconds)
         if args.guess_mols > 0:
@@ -408,6 +418,95 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def reduced_anchor(qb, ctx, oracle, thr, builds=20):
+    """The J/K build of the reduced workload (4 H + 2 heavy atoms at the bench workload's
+    density and basis statistics, 36 functions) timed in full on both sides: the GPU's
+    device-timed build and the oracle's Float64 restatement over every surviving shell
+    quartet on all host threads (no sampling, no extrapolation)."""
+    from quiqbox_gb300 import _lib as L
+    from quiqbox_gb300.workloads import random_density, reduced_shell_molecule
+    _, _, bs = reduced_shell_molecule()
+    fb = qb.flatten(bs)
+    n = fb.nfun
+    D = random_density(n, 3)
+    lib = ctx.lib
+    b = L.BasisArgs(fb)
+    Df = np.ascontiguousarray(D.reshape(-1, order="F"))
+    ctx.check(lib.qb_jk_prepare(ctx.h, b.ref(), thr))
+    ctx.check(lib.qb_jk_upload_density(ctx.h, L.dptr(Df)))
+    st = L.QBJKStats()
+    for _ in range(3):
+        ctx.check(lib.qb_jk_execute(ctx.h))
+    ms = []
+    for _ in range(builds):
+        ctx.check(lib.qb_jk_execute(ctx.h))
+        ctx.check(lib.qb_jk_get_stats(ctx.h, C.byref(st)))
+        ms.append(st.ms_last)
+    Jg = np.zeros(n * n)
+    Kg = np.zeros(n * n)
+    ctx.check(lib.qb_jk_download(ctx.h, L.dptr(Jg), L.dptr(Kg)))
+    arr = [np.zeros(st.npair, np.int32) for _ in range(4)]
+    Qv = np.zeros(st.npair)
+    npair = C.c_int()
+    ctx.check(lib.qb_jk_pair_table(ctx.h, C.byref(npair), *[L.iptr(a) for a in arr], L.dptr(Qv)))
+    classes = survivors((arr[0], arr[1], arr[2], arr[3], Qv), float(np.abs(D).max()), thr)
+    qs, gs = [], []
+    for cl in classes:
+        picks = [(i, j) for i in range(len(cl["bra"])) for j in range(int(cl["cnt"][i]))]
+        if picks:
+            q, g = expand((arr[0], arr[1], arr[2], arr[3], Qv), cl, picks)
+            qs.append(q)
+            gs.append(g)
+    q, g = np.concatenate(qs), np.concatenate(gs)
+    nthreads = oracle.num_threads()
+    t0 = time.perf_counter()
+    Jp, Kp = oracle.jk_list(fb, q, g, D, nthreads)
+    t_cpu = time.perf_counter() - t0
+    Jc, Kc = (Jp + Jp.T) / 4, (Kp + Kp.T) / 8
+    quartets = int(st.quartets)
+    gpu_ms = float(np.median(ms))
+    return {"workload": "4 H + 2 C/N/O in a 5.9 bohr cube (the bench workload's atom density and shells), "
+                        f"N={n}, Schwarz {thr:g}, seeded density",
+            "quartets": quartets, "gpu_ms_per_build": gpu_ms, "gpu_gquartets_per_s": quartets / gpu_ms * 1e-6,
+            "cpu_s_per_build": t_cpu, "cpu_gquartets_per_s": quartets / t_cpu * 1e-9, "cpu_cores": nthreads,
+            "cpu_kind": "port (oracle Float64, the reference's per-component recursions), every surviving quartet",
+            "max_abs_dJ_gpu_vs_cpu": float(np.abs(Jg.reshape((n, n), order="F") - Jc).max()),
+            "max_abs_dK_gpu_vs_cpu": float(np.abs(Kg.reshape((n, n), order="F") - Kc).max())}
+
+
+def config0(qb, oracle, solves=20):
+    """Config 0: RHF of H2O / STO-3G at the bench geometry (7 functions), core-Hamiltonian
+    guess, DIIS with the reference's default coefficient solver, |dE| <= 1e-10 Ha and
+    RMS(dD) <= 1e-8, through the public runHartreeFock call (host in, host out); the
+    oracle's restatement of the same run on the host beside it."""
+    from quiqbox_gb300.workloads import h2o
+    nuc, fb = h2o()
+    cfg = qb.HFconfig(initial="CoreH", strategy=qb.SCFconfig(("DIIS",), (1e-10,), secondaryConvRatio=(1e6, 100.0)))
+    for _ in range(2):
+        r = qb.runHartreeFock(nuc, fb, cfg)
+    t0 = time.perf_counter()
+    for _ in range(solves):
+        r = qb.runHartreeFock(nuc, fb, cfg)
+    t_gpu = (time.perf_counter() - t0) / solves
+    ro = oracle.hartree_fock(fb, nuc.charges, nuc.positions, 5, 5, guess="CoreH", methods=("DIIS",),
+                             intervals=(1e-10,), secondary=(1e6, 100.0))
+    t0 = time.perf_counter()
+    for _ in range(solves):
+        oracle.hartree_fock(fb, nuc.charges, nuc.positions, 5, 5, guess="CoreH", methods=("DIIS",),
+                            intervals=(1e-10,), secondary=(1e6, 100.0))
+    t_cpu = (time.perf_counter() - t0) / solves
+    return {"workload": "H2O, STO-3G, bench geometry (O at 0; H at (0, +-1.4305, 1.1093) bohr), N = 7; CoreH "
+                        "guess, DIIS (L-BFGS-B coefficients), |dE| <= 1e-10 Ha, RMS(dD) <= 1e-8",
+            "gpu_solves_per_s": 1.0 / t_gpu, "gpu_ms_per_solve": 1e3 * t_gpu, "iterations": int(r.steps),
+            "converged": bool(r.converged), "E_total": float(sum(r.energy)),
+            "abs_dE_vs_oracle": float(abs(r.energy[0] - ro["E_elec"])),
+            "oracle_iterations": int(ro["steps"]),
+            "cpu_solves_per_s": 1.0 / t_cpu, "cpu_ms_per_solve": 1e3 * t_cpu,
+            "cpu_kind": "port (oracle restatement of runHartreeFock, stored ERI tensor)",
+            "cpu_cores": int(oracle.num_threads()),
+            "note": "latency-bound (7 functions): one molecule, one SCF step per few dozen small kernels"}
 
 
 BATCH_WORKLOAD = ("batched RHF: seeded bonded chains of 2-16 atoms (H:C:N:O = 5:3:1:1, bonds 1.8-2.9 bohr, "

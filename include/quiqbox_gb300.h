@@ -187,6 +187,16 @@ int qb_jk_get_stats(qb_ctx* ctx, qb_jk_stats* stats);
  * function indices of the two shells (A is the shell of higher angular momentum). */
 int qb_jk_pair_table(qb_ctx* ctx, int* npair, int* fa, int* fb, int* la, int* lb, double* Q);
 
+/* J and K restricted to an explicit list of shell quartets (a test hook for the class
+ * kernels, no reference counterpart): the sum over the listed quartets of the terms the
+ * full build (qb_jk_execute, replacing getGcore, src/HartreeFock.jl:305-319) adds for them,
+ * with the density of the last qb_jk_upload_density and each class's current kernel
+ * variant.  pairs holds 2 * nq indices into the pair table of qb_jk_pair_table: bra pair,
+ * ket pair, in canonical order (the ket's pair class not above the bra's; within one class
+ * the ket index not above the bra index), else QB_ERR_ARG.  No Schwarz screening is
+ * applied to the listed quartets; the kernels' primitive screening is. */
+int qb_jk_quartet_list(qb_ctx* ctx, int64_t nq, const int* pairs, double* J, double* K);
+
 /* Hartree–Fock SCF (runHartreeFock, src/HartreeFock.jl:953-1228) on the GPU:
  * symmetric orthogonalisation, Jacobi diagonalisation, direct J/K Fock build,
  * DD / DIIS / EDIIS / ADIIS convergence methods with the reference's three DIIS
@@ -309,7 +319,13 @@ int qb_fp64_peak(qb_ctx* ctx, double* tflops);
  *    other host threads) race and corrupt each other's results.
  *  - Bad basis data returns QB_ERR_ARG (pointer layout), QB_ERR_UNSUPPORTED
  *    (angular momentum > 12) or QB_ERR_DOMAIN (exponent <= 0).  No context, so no
- *    qb_last_error() message. */
+ *    qb_last_error() message.
+ *  - The call waits on `stream` three times (after each of the two input checks and for
+ *    the final status), so it returns with its work finished.
+ *  - Cost: it evaluates every canonical function quartet (about nfun^4/8) without
+ *    screening, far more work than qb_jk's shell-quartet kernels: measured on a GB300 with
+ *    s/p/d bases, 1.8 s per call at nfun = 100 and 26 s at nfun = 200 (qb_jk, unscreened:
+ *    0.05 s and 0.16 s).  It suits small bases. */
 int qb_jk_noalloc(const qb_basis* dbasis, const double* dD, double* dJ, double* dK, void* stream);
 
 #ifdef __cplusplus

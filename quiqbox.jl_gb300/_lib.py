@@ -24,7 +24,7 @@ EXPORTED = ["qb_create", "qb_destroy", "qb_last_error", "qb_device_info", "qb_ov
             "qb_batch_config_default", "qb_run_rhf_batched", "qb_jk_autotune",
             "qb_bf16_gemm_nt", "qb_gelu_forward", "qb_gelu_backward", "qb_f32_to_bf16", "qb_bf16_transpose",
             "qb_colsum", "qb_mse_grad", "qb_adam_step", "qb_adjoint_jk", "qb_eigh_lowest",
-            "qb_guess_features", "qb_guess_assemble", "qb_diis_coefficients"]
+            "qb_guess_features", "qb_guess_assemble", "qb_diis_coefficients", "qb_jk_quartet_list"]
 
 
 class DimensionMismatch(ValueError):
@@ -103,6 +103,7 @@ def load():
         L.qb_jk_get_stats.argtypes = [vp, C.POINTER(QBJKStats)]
         pi = C.POINTER(C.c_int)
         L.qb_jk_pair_table.argtypes = [vp, pi, pi, pi, pi, pi, pd]
+        L.qb_jk_quartet_list.argtypes = [vp, C.c_int64, pi, pd, pd]
         L.qb_scf_config_default.argtypes = [C.POINTER(QBSCFConfig)]
         L.qb_scf_config_default.restype = None
         L.qb_run_hartree_fock.argtypes = [vp, pb, C.c_int, pd, pd, C.c_int, C.c_int, C.POINTER(QBSCFConfig),

@@ -293,6 +293,14 @@ int qb_jk_execute(qb_ctx* ctx) {
     return QB_OK;
 }
 
+int qb_jk_quartet_list(qb_ctx* ctx, int64_t nq, const int* pairs, double* J, double* K) {
+    QB_TRY(enter(ctx));
+    if (!ctx->jk_prepared) return qb_set_error(ctx, QB_ERR_ARG, "call qb_jk_prepare first");
+    if (nq < 0 || (nq > 0 && !pairs)) return qb_set_error(ctx, QB_ERR_ARG, "bad quartet list");
+    QB_TRY(qb_jk_quartets_device(ctx, (long long)nq, pairs, ctx->d_J.p, ctx->d_K.p));
+    return qb_jk_download(ctx, J, K);
+}
+
 int qb_jk_autotune(qb_ctx* ctx, int repeats, int* variants) {
     QB_TRY(enter(ctx));
     return qb_jk_autotune_device(ctx, repeats, variants);

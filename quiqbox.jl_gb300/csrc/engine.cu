@@ -568,6 +568,59 @@ int qb_jk_device(qb_ctx* ctx, const double* dD, double* dJ, double* dK, double t
     return qb_cuda_check(ctx, cudaGetLastError(), "J/K finalize");
 }
 
+// J/K restricted to an explicit list of canonical shell quartets (pair indices into the
+// pair table, bra pair class >= ket pair class, ket index <= bra index within one class):
+// each quartet is one launch of its class's production kernel (the context's variant)
+// over a one-bra, one-ket work list, accumulated into the same J'/K' and finalised as a
+// full build is.  For parity tests of the class kernels on chosen quartets.
+int qb_jk_quartets_device(qb_ctx* ctx, long long nq, const int* pq, double* dJ, double* dK) {
+    cudaStream_t s = ctx->stream;
+    const int n = ctx->nfun;
+    const size_t nn = (size_t)n * n;
+    if (!ctx->shell_path) return qb_set_error(ctx, QB_ERR_UNSUPPORTED, "the basis is not on the shell path");
+    QB_TRY(qb_ensure_pairs(ctx));
+    const int npair = ctx->pc_off[ctx->npc];
+    auto pc_of = [&](int p) {
+        int pc = 0;
+        while (pc + 1 <= ctx->npc && ctx->pc_off[pc + 1] <= p) ++pc;
+        return pc;
+    };
+    std::vector<int> cls(nq);
+    for (long long q = 0; q < nq; ++q) {
+        const int P = pq[2 * q], Q = pq[2 * q + 1];
+        if (P < 0 || P >= npair || Q < 0 || Q >= npair) return qb_set_error(ctx, QB_ERR_ARG, "pair index out of range");
+        const int X = pc_of(P), Y = pc_of(Q);
+        int c = -1;
+        for (int k = 0; k < ctx->nclass; ++k)
+            if (ctx->class_bra[k] == X && ctx->class_ket[k] == Y) c = k;
+        if (c < 0 || (X == Y && Q > P)) return qb_set_error(ctx, QB_ERR_ARG, "quartet not in canonical order");
+        cls[q] = c;
+    }
+    QB_CUDA(ctx, ctx->d_Dt.ensure(nn));
+    QB_CUDA(ctx, ctx->d_Jp.ensure(nn));
+    QB_CUDA(ctx, ctx->d_Kp.ensure(nn));
+    QB_CUDA(ctx, ctx->d_dmax.ensure(1));
+    QB_CUDA(ctx, ctx->d_one_offs.ensure(2));
+    const long long one[2] = {0, 1};
+    QB_CUDA(ctx, cudaMemcpyAsync(ctx->d_one_offs.p, one, sizeof(one), cudaMemcpyHostToDevice, s));
+    QB_CUDA(ctx, cudaMemsetAsync(ctx->d_Jp.p, 0, nn * sizeof(double), s));
+    QB_CUDA(ctx, cudaMemsetAsync(ctx->d_Kp.p, 0, nn * sizeof(double), s));
+    QB_CUDA(ctx, cudaMemsetAsync(ctx->d_dmax.p, 0, sizeof(double), s));
+    QB_CUDA(ctx, cudaMemsetAsync(ctx->d_primcount.p, 0, QB_MAX_CLASS * sizeof(unsigned long long), s));
+    qb_density_prescale(s, n, ctx->d_ratio.p, ctx->d_D.p, ctx->d_Dt.p, ctx->d_dmax.p);
+    ctx->last_execute_shell = false;   // the class statistics of qb_jk_get_stats stay those of a full build
+    for (long long q = 0; q < nq; ++q) {
+        const int P = pq[2 * q], Q = pq[2 * q + 1], c = cls[q];
+        const ClassWork w{ctx->d_pairs.p + P, ctx->d_pairs.p + Q, ctx->d_one_offs.p, 1, P == Q ? 1 : 0};
+        const JKArgs args{ctx->d_prims.p, ctx->d_prims32.p, ctx->boys.p, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p,
+                          ctx->d_primcount.p + c, n};
+        ctx->launch[c].jk[ctx->variant[c]](w, args, 1, s);
+    }
+    QB_CUDA(ctx, cudaGetLastError());
+    qb_jk_finalize(s, n, ctx->d_ratio.p, ctx->d_Jp.p, ctx->d_Kp.p, dJ, dK);
+    return qb_cuda_check(ctx, cudaGetLastError(), "J/K finalize");
+}
+
 // Autotuner: after one J/K build on the current basis and density (work lists in place),
 // time every compiled kernel variant of every class with work on the same list (CUDA events
 // on the context stream, best of `repeats`) and keep the fastest per class.

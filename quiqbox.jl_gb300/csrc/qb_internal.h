@@ -83,6 +83,7 @@ int qb_build_prim_pairs(cudaStream_t s, const PairSlot* d_slots, int nslot, cons
                         PrimPair* d_prims, float4* d_prims32, int* d_nkept, unsigned long long* d_kmax);
 
 int qb_jk_autotune_device(qb_ctx* ctx, int repeats, int* chosen);
+int qb_jk_quartets_device(qb_ctx* ctx, long long nq, const int* pq, double* dJ, double* dK);
 int qb_lowest_eig(cudaStream_t s, int n, int k, double* A, double* Y, double* w, double* work);
 int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nnuc, const double* Z,
                      const double* R, const int* nocc, const qb_batch_config* cfg, qb_batch_result* res);
@@ -134,6 +135,7 @@ struct qb_ctx {
     int class_bra[QB_MAX_CLASS] = {}, class_ket[QB_MAX_CLASS] = {};
     long long offs_off[QB_MAX_CLASS + 1] = {};
     DevArray<long long> d_offs;
+    DevArray<long long> d_one_offs;       // {0, 1}: the work list of one quartet
     DevArray<long long> d_stats;          // 2 per class: quartets, primitive quartets (upper bound)
     DevArray<unsigned long long> d_primcount;   // per class: primitive quartets evaluated
 

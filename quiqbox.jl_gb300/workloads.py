@@ -42,6 +42,14 @@ def random_shell_molecule(n_h=64, n_heavy=16, box=14.0, min_dist=1.3, heavy=("C"
     return atoms, [tuple(float(v) for v in c) for c in coords], basis
 
 
+def reduced_shell_molecule(n_h=4, n_heavy=2, seed=3):
+    """The ERI + J/K workload's statistics at a size the quad-precision oracle can check in
+    full: the same atoms per volume (80 atoms per (14 bohr)^3), minimum distance, shell
+    sets, exponent and coefficient ranges, in a cube holding n_h + n_heavy atoms."""
+    box = 14.0 * ((n_h + n_heavy) / 80.0) ** (1.0 / 3.0)
+    return random_shell_molecule(n_h=n_h, n_heavy=n_heavy, box=box, seed=seed)
+
+
 def random_density(n, seed=0):
     """Symmetric positive semidefinite D = A A^T / n, A uniform in [-1, 1]."""
     rng = np.random.default_rng(seed + 7919)

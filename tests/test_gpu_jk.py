@@ -179,3 +179,113 @@ def test_jk_autotune_keeps_results(qb, oracle):
     scale = max(np.abs(Jr).max(), 1.0)
     assert np.abs(J - Jr).max() < 1e-12 * scale
     assert np.abs(K - Kr).max() < 1e-12 * scale
+
+
+# ---------------------------------------------------------------------------
+# Parity at the bench workload's own size and screening (64 H + 16 heavy atoms, N = 416,
+# Schwarz 1e-12, primitive-quartet screening on): the production class kernels evaluated
+# on a stratified sample of the surviving shell quartets against the quad-precision
+# oracle on the same quartets, and the full build of a reduced workload with the same
+# statistics against the oracle's exact J and K (tests/golden/c1_reduced_jk.json).
+
+def _ncart(L):
+    return (L + 1) * (L + 2) // 2
+
+
+def _pair_table(qb, ctx, fb, D, schwarz):
+    import ctypes as C
+    from quiqbox_gb300 import _lib as L
+    b = L.BasisArgs(fb)
+    Df = np.ascontiguousarray(D.reshape(-1, order="F"))
+    ctx.check(ctx.lib.qb_jk_prepare(ctx.h, b.ref(), schwarz))
+    ctx.check(ctx.lib.qb_jk_upload_density(ctx.h, L.dptr(Df)))
+    npair = C.c_int()
+    ctx.check(ctx.lib.qb_jk_pair_table(ctx.h, C.byref(npair), None, None, None, None, None))
+    arr = [np.zeros(npair.value, np.int32) for _ in range(4)]
+    Q = np.zeros(npair.value)
+    ctx.check(ctx.lib.qb_jk_pair_table(ctx.h, C.byref(npair), *[L.iptr(a) for a in arr], L.dptr(Q)))
+    return b, arr[0], arr[1], arr[2], arr[3], Q
+
+
+def _stratified_survivors(fa, fb_, la, lb, Q, dmax, thr, rng, fq_budget=5000, min_per_class=8):
+    """Canonical surviving shell quartets (global pair indices, bra class >= ket class, ket
+    index <= bra index within a class), sampled per class: as many as fq_budget function
+    quartets allow, at least min_per_class."""
+    pcs = sorted(set(zip(la.tolist(), lb.tolist())), key=lambda t: t[0] * (t[0] + 1) // 2 + t[1])
+    idx = {pc: np.where((la == pc[0]) & (lb == pc[1]))[0] for pc in pcs}
+    picks, per_class = [], {}
+    for x, X in enumerate(pcs):
+        for Y in pcs[:x + 1]:
+            bi, ki = idx[X], idx[Y]
+            cand = []
+            for ii, P in enumerate(bi):
+                kmax = len(ki) if X != Y else ii + 1
+                ok = np.where(Q[P] * Q[ki[:kmax]] * dmax >= thr)[0]
+                cand.extend((int(P), int(ki[j])) for j in ok)
+            if not cand:
+                continue
+            fq = _ncart(X[0]) * _ncart(X[1]) * _ncart(Y[0]) * _ncart(Y[1])
+            k = min(len(cand), max(min_per_class, fq_budget // fq))
+            sel = rng.choice(len(cand), k, replace=False)
+            picks.extend(cand[i] for i in sel)
+            per_class[X + Y] = k
+    return picks, per_class
+
+
+def _expand_pairs(picks, fa, fb_, la, lb):
+    """Shell quartets -> function quartets with the degeneracy weights of the build."""
+    q, g = [], []
+    for P, R in picks:
+        deg = (1.0 if fa[P] == fb_[P] else 2.0) * (1.0 if fa[R] == fb_[R] else 2.0) * (1.0 if P == R else 2.0)
+        for a in range(_ncart(la[P])):
+            for b in range(_ncart(lb[P])):
+                for c in range(_ncart(la[R])):
+                    for d in range(_ncart(lb[R])):
+                        q.append((fa[P] + a, fb_[P] + b, fa[R] + c, fb_[R] + d))
+                        g.append(deg)
+    return np.asarray(q, np.int32), np.asarray(g)
+
+
+def test_bench_workload_quartets_vs_exact_oracle(qb, oracle):
+    import ctypes as C
+    from quiqbox_gb300 import _lib as L
+    from quiqbox_gb300.workloads import random_density, random_shell_molecule
+    _, _, bs = random_shell_molecule(seed=0)
+    fb = qb.flatten(bs)
+    n = fb.nfun
+    D = random_density(n, 0)
+    ctx = qb.Context(0)
+    _, fa, fb_, la, lb, Q = _pair_table(qb, ctx, fb, D, 1e-12)
+    rng = np.random.default_rng(2024)
+    picks, per_class = _stratified_survivors(fa, fb_, la, lb, Q, float(np.abs(D).max()), 1e-12, rng)
+    assert len(per_class) == 21 and len(picks) > 9000
+    pq = np.ascontiguousarray(np.asarray(picks, np.int32).reshape(-1))
+    J = np.zeros(n * n)
+    K = np.zeros(n * n)
+    ctx.check(ctx.lib.qb_jk_quartet_list(ctx.h, len(picks), L.iptr(pq), L.dptr(J), L.dptr(K)))
+    J = J.reshape((n, n), order="F")
+    K = K.reshape((n, n), order="F")
+    q, g = _expand_pairs(picks, fa, fb_, la, lb)
+    Jp, Kp = oracle.jk_list(fb, q, g, D, 0, exact=True)
+    Jx, Kx = (Jp + Jp.T) / 4, (Kp + Kp.T) / 8
+    assert np.abs(J - Jx).max() < 1e-12, np.abs(J - Jx).max()
+    assert np.abs(K - Kx).max() < 1e-12, np.abs(K - Kx).max()
+    ctx.close()
+
+
+def test_reduced_bench_workload_full_build_vs_exact(qb):
+    import json
+    from pathlib import Path
+    from quiqbox_gb300.basis import FlatBasis
+    fx = json.loads((Path(__file__).parent / "golden" / "c1_reduced_jk.json").read_text())
+    n = fx["nfun"]
+    fb = FlatBasis(np.asarray(fx["fun_ptr"], np.int32), np.asarray(fx["center"]).reshape(-1, 3),
+                   np.asarray(fx["ijk"], np.int32).reshape(-1, 3), np.asarray(fx["alpha"]), np.asarray(fx["weight"]))
+    D = np.asarray(fx["D_colmajor"]).reshape((n, n), order="F")
+    Jx = np.asarray(fx["J_colmajor"]).reshape((n, n), order="F")
+    Kx = np.asarray(fx["K_colmajor"]).reshape((n, n), order="F")
+    scale = np.abs(Jx).max()
+    for thr in (0.0, 1e-12):   # unscreened, and with the bench workload's Schwarz threshold
+        J, K = qb.jk(fb, D, schwarz=thr)
+        assert np.abs(J - Jx).max() < 1e-12 * scale, (thr, np.abs(J - Jx).max())
+        assert np.abs(K - Kx).max() < 1e-12 * scale, (thr, np.abs(K - Kx).max())
