@@ -532,6 +532,7 @@ def batched_rhf(qb, n_mol, seed, cpu_seconds):
            "nfun_mean": float(res.nfun.mean()), "nfun_max": int(res.nfun.max()),
            "converged": int(conv.sum()), "solves_per_s": float(conv.sum() / wall),
            "unit": "converged RHF solves/s (whole batch: host preparation + integrals + SCF)",
+           "strategy": "SCFconfig((:DIIS,), (1e-10,), Dict(1=>[:solver=>:LCM])), RMS(dD) <= 1e-8, CoreH guess",
            "wall_s": wall, "ms_integrals": res.ms_integrals, "ms_scf": res.ms_scf,
            "mean_iterations_converged": float(res.iterations[conv].mean()) if conv.any() else None,
            "graph_launches": res.graph_launches, "stored_quartets": res.quartets,
@@ -561,6 +562,19 @@ def batched_rhf(qb, n_mol, seed, cpu_seconds):
                            "sample": f"{done} random molecules of the batch ({cpu_conv} converged), "
                                      f"{t_cpu:.1f} s of CPU work"}
     out["max_abs_dE_vs_oracle_on_sample"] = float(max(diffs)) if diffs else None
+    # the reference's default SCF strategy on the same molecules: (DD, ADIIS, DIIS) with
+    # thresholds (5e-3, 1e-4, 1e-10) and L-BFGS-B coefficients (HartreeFock.jl:17,27)
+    cfg = qb.BatchSCFConfig(strategy=qb.SCFconfig.default(threshold=1e-10))
+    qb.runHartreeFockBatched(args[:8], config=cfg)
+    t0 = time.perf_counter()
+    rd = qb.runHartreeFockBatched(args, config=cfg)
+    wd = time.perf_counter() - t0
+    out["reference_default_strategy"] = {
+        "strategy": "SCFconfig(threshold=1e-10): (DD, ADIIS, DIIS), (5e-3, 1e-4, 1e-10), L-BFGS-B, "
+                    "secondaryConvRatio (1000, 1000), core-Hamiltonian guess",
+        "converged": int(rd.converged.sum()), "solves_per_s": float(rd.converged.sum() / wd), "wall_s": wd,
+        "ms_scf": rd.ms_scf, "graph_launches": rd.graph_launches,
+        "mean_iterations_converged": float(rd.iterations[rd.converged].mean()) if rd.converged.any() else None}
     return out
 
 

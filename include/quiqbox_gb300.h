@@ -243,12 +243,17 @@ int qb_run_hartree_fock(qb_ctx* ctx, const qb_basis* basis, int nnuc, const doub
 /* Batched closed-shell Hartree–Fock over many independent molecules in one call.
  * The reference solves one molecule per runHartreeFock (src/HartreeFock.jl:953-1046);
  * this runs hundreds of them together: integrals of all molecules once (screened ERI
- * blocks stored on the device), then CUDA-graph-captured SCF iterations, each one batched
- * launch per step for every molecule not yet converged.  Per molecule: a flattened basis
- * of s and p Cartesian shells (1 <= nfun <= 256), nnuc[m] nuclei (charges and positions
- * concatenated over molecules in Z and R), nocc[m] doubly occupied orbitals.  Core-
- * Hamiltonian guess, symmetric orthogonalisation, Pulay DIIS; converged when
- * |dE| <= conv_energy and RMS(dD_total) <= conv_density.  energy[m] receives the
+ * blocks stored on the device), then every SCF iteration of every molecule in one launch
+ * of a CUDA graph whose conditional while-node repeats (digest, step) passes until no
+ * molecule iterates.  Per molecule: a flattened basis of s and p Cartesian shells
+ * (1 <= nfun <= 256), nnuc[m] nuclei (charges and positions concatenated over molecules in
+ * Z and R), nocc[m] doubly occupied orbitals.  Core-Hamiltonian guess (or initial_density),
+ * symmetric orthogonalisation, then runHartreeFockCore's method sequence
+ * (src/HartreeFock.jl:1049-1228) per molecule: nmethod = 0 runs one DIIS method with exact
+ * (Lagrange-multiplier) coefficients, converged when |dE| <= conv_energy and
+ * RMS(dD_total) <= conv_density; nmethod >= 1 runs the given methods, thresholds and
+ * coefficient solvers with the reference's convergence, oscillation and early-stop rules,
+ * e.g. its default SCFconfig (DD, ADIIS, DIIS) with L-BFGS-B.  energy[m] receives the
  * electronic energy (add the nuclear repulsion for the total). */
 typedef struct {
     double conv_energy;     /* default 1e-10 Ha */
@@ -268,6 +273,14 @@ typedef struct {
                                iterations restarts from the core-Hamiltonian guess in the same call
                                (the iterations of both attempts count against max_iter); 0: never
                                (default) */
+    int nmethod;            /* 0 (default): the single DIIS method above; 1..8: the strategy below */
+    int method[8];          /* QB_SCF_* per method (as qb_scf_config)                            */
+    double interval[8];     /* per-method thresholds; the last converges                         */
+    int solver[8];          /* QB_DIIS_* per method (default LBFGS)                               */
+    double secondary_ratio[2];   /* RMS(FDS-SDF) and RMS(dD) ratios (default 1000, 1000)         */
+    double oscillate_threshold;  /* default 5e-6                                                 */
+    int early_stop;         /* default 1                                                          */
+    double damp_strength;   /* DD damping, default 0.75                                           */
 } qb_batch_config;
 
 typedef struct {
@@ -280,7 +293,7 @@ typedef struct {
     int64_t quartets;       /* stored shell quartets */
     int64_t prim_quartets;  /* primitive quartets evaluated for them */
     int64_t eri_doubles;    /* stored integrals */
-    int graph_launches;
+    int graph_launches;     /* 1: the whole iteration ran as one graph launch */
     double* density;        /* NULL or room for the final per-spin densities, concatenated */
     int* restarted;         /* NULL or nmol: 1 if the molecule restarted from the core-Hamiltonian guess */
 } qb_batch_result;

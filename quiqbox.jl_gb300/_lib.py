@@ -171,7 +171,9 @@ class QBBatchConfig(C.Structure):
     _fields_ = [("conv_energy", C.c_double), ("conv_density", C.c_double), ("max_iter", C.c_int),
                 ("diis_size", C.c_int), ("schwarz", C.c_double), ("iters_per_graph", C.c_int),
                 ("initial_density", C.POINTER(C.c_double)), ("eigensolver", C.c_int), ("jacobi_sweeps", C.c_int),
-                ("fallback_iter", C.c_int)]
+                ("fallback_iter", C.c_int), ("nmethod", C.c_int), ("method", C.c_int * 8),
+                ("interval", C.c_double * 8), ("solver", C.c_int * 8), ("secondary_ratio", C.c_double * 2),
+                ("oscillate_threshold", C.c_double), ("early_stop", C.c_int), ("damp_strength", C.c_double)]
 
 
 class QBBatchResult(C.Structure):

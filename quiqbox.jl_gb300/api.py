@@ -398,6 +398,10 @@ class BatchSCFConfig:
     eigensolver: int = 0          # 0: tridiagonal occupied-subspace solver; 1: Jacobi
     jacobi_sweeps: int = 0        # Jacobi sweeps per SCF iteration; 0 = to convergence
     fallback_iter: int = 0        # with initial densities: restart from CoreH after this many iterations
+    strategy: Optional[SCFconfig] = None   # None: one DIIS method at conv_energy, exact coefficients;
+                                           # else the reference's method sequence, e.g. SCFconfig.default(1e-10)
+    earlyStop: bool = True
+    dampStrength: float = 0.75
 
 
 @dataclass
@@ -452,7 +456,8 @@ def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ct
     molecules: sequence of (nucInfo, basis) or (nucInfo, basis, charge); nucInfo a
     NuclearCluster, basis a list of orbitals or a FlatBasis.  Each molecule is what
     runHartreeFock (HartreeFock.jl:972-1046) would solve with initial=:CoreH and the
-    :DIIS method, all of them sharing every launch."""
+    strategy of ``config`` (default: :DIIS with exact coefficients), all of them sharing
+    every launch."""
     c = _ctx(ctx)
     cfg = config or BatchSCFConfig()
     nmol = len(molecules)
@@ -495,9 +500,25 @@ def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ct
                 raise DimensionMismatch("initial density shape")
             parts.append(D.reshape(-1, order="F"))
         d0 = np.ascontiguousarray(np.concatenate(parts))
-    qcfg = L.QBBatchConfig(cfg.conv_energy, cfg.conv_density, cfg.max_iter, cfg.diis_size, cfg.schwarz,
-                           cfg.iters_per_graph, L.dptr(d0) if d0 is not None else d0_dev, cfg.eigensolver,
-                           cfg.jacobi_sweeps, cfg.fallback_iter)
+    qcfg = L.QBBatchConfig()
+    c.lib.qb_batch_config_default(C.byref(qcfg))
+    qcfg.conv_energy, qcfg.conv_density, qcfg.max_iter = cfg.conv_energy, cfg.conv_density, cfg.max_iter
+    qcfg.diis_size, qcfg.schwarz, qcfg.iters_per_graph = cfg.diis_size, cfg.schwarz, cfg.iters_per_graph
+    qcfg.initial_density = L.dptr(d0) if d0 is not None else d0_dev
+    qcfg.eigensolver, qcfg.jacobi_sweeps, qcfg.fallback_iter = cfg.eigensolver, cfg.jacobi_sweeps, cfg.fallback_iter
+    qcfg.early_stop, qcfg.damp_strength = int(bool(cfg.earlyStop)), float(cfg.dampStrength)
+    if cfg.strategy is not None:
+        st = cfg.strategy
+        if len(st.methods) > 8:
+            raise ValueError("at most 8 SCF methods")
+        qcfg.nmethod = len(st.methods)
+        for k, (m, iv) in enumerate(zip(st.methods, st.intervals)):
+            qcfg.method[k] = _METHODS[m]
+            qcfg.interval[k] = float(iv)
+            qcfg.solver[k] = _SOLVERS[st.solver_of(k)]
+        qcfg.secondary_ratio[0] = float(st.secondaryConvRatio[0])
+        qcfg.secondary_ratio[1] = float(st.secondaryConvRatio[1])
+        qcfg.oscillate_threshold = float(st.oscillateThreshold)
     E = np.zeros(nmol)
     it = np.zeros(nmol, np.int32)
     conv = np.zeros(nmol, np.int32)

@@ -26,6 +26,7 @@
 #include <vector>
 #include "qb_internal.h"
 #include "qb_dense.cuh"
+#include "qb_diis_solvers.cuh"
 #include "eri_class_0000.cuh"
 #include "eri_class_1000.cuh"
 #include "eri_class_1010.cuh"
@@ -42,7 +43,6 @@
 
 #define QB_BATCH_MAXN 256
 #define QB_BATCH_DIIS 15                   // largest DIIS subspace (defaultDIISsize, HartreeFock.jl:16)
-#define QB_BATCH_SLOTS (QB_BATCH_DIIS + 1) // history slots: the subspace plus the entry being added
 #define QB_BATCH_RESET 4e-13               // resetThreshold = 1000 getAtolVal(Float64) (HartreeFock.jl:1337)
 #define QB_BATCH_NCLASS 6
 #define QB_BATCH_THREADS 256
@@ -69,21 +69,36 @@ struct DigestChunk {
 #define QB_DIGEST_CHUNK 2048        // quartets per digest block of a molecule with much work in a class
 #define QB_DIGEST_CHUNK_SMALL 512   // ... and of the others (enough blocks to spread a straggler)
 
+#define QB_BATCH_POOL 32   // entry slots of a molecule: history (<= 15) and DIIS subspace (<= 16) share them
+#define QB_BATCH_HIST 15   // history kept for the next method's start: max(3, DIISsize) entries
+
 struct MolDev {
-    int n, nocc, conv, iter;   // conv: 0 iterating, 1 converged, 2 stopped at max_iter, 3 failed
-    int dlen, sweeps;          // DIIS subspace: dlist[0..dlen) slot ids, oldest first
-    int iter0, restarted;      // iterations before a restart from the core-Hamiltonian guess
-    int dlist[QB_BATCH_SLOTS];
-    double dEs[QB_BATCH_SLOTS];   // per-spin energy of each slot's entry
-    double E, Eprev, dE, rmsD;
-    double *S, *H, *X, *F, *D, *Dt, *Do, *Jp, *Kp, *Cp, *W1, *W2, *W3, *W4, *W5, *W6;
-    double *Fh, *Eh, *B, *eps, *wt;
+    int n, nocc, conv, iter;   // conv: 0 iterating, 1 converged, 2 stopped, 3 failed; iter: step-kernel calls
+    int steps, stage, nstep, phase;   // SCF steps (the reference's i), method index, steps of the method,
+                                      // phase 0: the digested density is a step's entry, 1: a DD half step
+    int hlen, slen, ne, nde;   // history / subspace lengths, energies seen (Etots), energy changes seen
+    int iter0, restarted, sweeps, stale;   // stale: the history's last entry is not the digested density
+    int hlist[QB_BATCH_HIST + 1], slist[QB_BATCH_DIIS + 2];   // slot ids, oldest first
+    double sE[QB_BATCH_POOL];       // per-spin energy of each slot's entry
+    double c[QB_BATCH_DIIS + 2];    // the method's coefficient vector (carried between its steps)
+    double Er[32], dEr[4];          // last total energies (Etots) and energy changes (rings)
+    double E, Eprev, dE, rmsD, dF;
+    double *S, *H, *X, *Sh, *F, *D, *Dt, *Do, *Jp, *Kp, *Cp, *W1, *W2, *W3, *W4, *W5, *W6;
+    double *Fs, *Ds, *Es;           // per slot: F (AO), D (AO), e' = X^T (F D S - S D F) X
+    double *Gee, *Gdf;              // pool x pool: <e'_a, e'_b>, <D_a, F_b>
+    double *eps, *wt;
     const double* ratio;
+    QbDiisWork* dw;
 };
 
 struct StepParams {
-    double thr_e, thr_d;
-    int max_iter, diis, sweeps, eig;   // eig 0: tridiagonal occupied-subspace solver, 1: Jacobi
+    int nmethod;
+    int method[8];
+    double interval[8];
+    int solver[8];
+    double r1, r2, osc, damp;          // secondaryConvRatio, oscillateThreshold, dampStrength
+    int max_iter, diis, early_stop;
+    int sweeps, eig;                   // eig 0: tridiagonal occupied-subspace solver, 1: Jacobi
     int fallback;                      // > 0: restart from the core-Hamiltonian guess after this many
 };
 
@@ -229,36 +244,35 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_orth_kernel(MolDev*
         }
     }
     __syncthreads();
+    // S^{1/2} = S X (orthonormal-basis densities D' = S^{1/2} D S^{1/2})
+    qb_cta_gemm(false, false, n, n, n, 1.0, M.S, n, M.X, n, 0.0, M.Sh, n);
     if (have_d0) {
-        // S^{1/2} = S X (W1), D' = W1 D0 W1^T
-        qb_cta_gemm(false, false, n, n, n, 1.0, M.S, n, M.X, n, 0.0, M.W1, n);
-        qb_cta_gemm(false, false, n, n, n, 1.0, M.W1, n, M.D, n, 0.0, M.W2, n);
-        qb_cta_gemm(false, true, n, n, n, 1.0, M.W2, n, M.W1, n, 0.0, M.Do, n);
+        qb_cta_gemm(false, false, n, n, n, 1.0, M.Sh, n, M.D, n, 0.0, M.W2, n);
+        qb_cta_gemm(false, true, n, n, n, 1.0, M.W2, n, M.Sh, n, 0.0, M.Do, n);
         for (int idx = tid; idx < nn; idx += nt) {
             const int i = idx % n, j = idx / n;
             M.Dt[idx] = M.D[idx] * M.ratio[i] * M.ratio[j];
         }
-        if (tid == 0) M.iter = 1;
+        if (tid == 0) M.iter = 1;   // the supplied density is the first entry (initializeSCF)
     }
 }
 
-// Pulay DIIS coefficients c (m entries) from the error Gram matrix B (ld QB_BATCH_SLOTS) of
-// the slots in idx: minimise c^T B c subject to sum c = 1 (DIIScore with v = 0,
-// HartreeFock.jl:1301-1315; the minimiser the constraint solvers converge to) via the
-// bordered linear system, Gaussian elimination with partial pivoting (largest |pivot|,
-// lowest row on ties; singular below 1e-14 after scaling by max B_ii) by one warp: lane i
-// holds row i in shared memory A and the rows of each elimination step update in
-// parallel.  Every lane of the warp calls it; the result is warp-uniform; false if singular.
+// Pulay DIIS coefficients c (m entries) minimising c^T B c with sum c = 1, B the error Gram
+// matrix of the pool slots idx (leading dimension QB_BATCH_POOL): DIIScore with v = 0
+// (HartreeFock.jl:1301-1315) solved exactly, the solution CMsolver! gives (:1445-1477),
+// via the bordered linear system by one warp: Gaussian elimination with partial pivoting
+// (largest |pivot|, lowest row on ties; singular below 1e-14 after scaling by max B_ii),
+// lane i holding row i in shared memory A.  Every lane calls it; false if singular.
 __device__ bool qb_diis_coeffs_warp(int m, const double* B, const int* idx, double* c,
-                                    double (*A)[QB_BATCH_SLOTS + 2]) {
+                                    double (*A)[QB_BATCH_DIIS + 3]) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, n = m + 1;
     double scale = 0.0;
-    for (int i = 0; i < m; ++i) scale = fmax(scale, fabs(B[idx[i] * QB_BATCH_SLOTS + idx[i]]));
+    for (int i = 0; i < m; ++i) scale = fmax(scale, fabs(B[idx[i] * QB_BATCH_POOL + idx[i]]));
     if (!(scale > 0.0)) return false;
     if (lane < n) {
         for (int j = 0; j < n; ++j)
-            A[lane][j] = lane < m ? (j < m ? B[idx[lane] * QB_BATCH_SLOTS + idx[j]] / scale : 1.0) : (j < m ? 1.0 : 0.0);
+            A[lane][j] = lane < m ? (j < m ? B[idx[lane] * QB_BATCH_POOL + idx[j]] / scale : 1.0) : (j < m ? 1.0 : 0.0);
         A[lane][n] = lane < m ? 0.0 : 1.0;   // right-hand side
     }
     __syncwarp();
@@ -299,132 +313,13 @@ __device__ bool qb_diis_coeffs_warp(int m, const double* B, const int* idx, doub
     return true;
 }
 
-// One SCF iteration of one molecule per thread block (blocks ordered by size, largest first).
-__global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev* mols, const int* __restrict__ order,
-                                                                         const StepParams prm, int* active) {
-    __shared__ QbJacobiSmem<QB_BATCH_MAXN> jsm;
-    __shared__ QbEigSmem<QB_BATCH_MAXN> esm;
-    __shared__ double red[33];
-    __shared__ double s_c[QB_BATCH_SLOTS];
-    __shared__ int s_idx[QB_BATCH_SLOTS], s_ok;
-    __shared__ double s_diis[QB_BATCH_SLOTS][QB_BATCH_SLOTS + 2];
-    MolDev& M = mols[order[blockIdx.x]];
-    if (M.conv) return;
+// eigenvectors of the occupied orbitals of F' (in W2, orthonormal basis, destroyed) -> the
+// density D' = Y Y^T (W3) and D = (X Y)(X Y)^T (W2)
+__device__ int qb_batch_density(MolDev& M, const StepParams& prm, QbJacobiSmem<QB_BATCH_MAXN>& jsm,
+                                QbEigSmem<QB_BATCH_MAXN>& esm) {
     const int n = M.n, nn = n * n, tid = threadIdx.x, nt = blockDim.x;
-    const int it = M.iter;
-    const double* r = M.ratio;
-    double E = 0.0;
-    if (it == 0) {
-        // core-Hamiltonian guess (also after a restart: drop what the digest accumulated)
-        for (int i = tid; i < nn; i += nt) {
-            M.F[i] = M.H[i];
-            M.Jp[i] = 0.0;
-            M.Kp[i] = 0.0;
-        }
-        __syncthreads();
-    } else {
-        // F = H + 2J - K (libint-convention accumulators, per-function ratios), energy of D
-        double e = 0.0;
-        for (int idx = tid; idx < nn; idx += nt) {
-            const int i = idx % n, j = idx / n;
-            const double rr = r[i] * r[j];
-            const double J = 0.25 * rr * (M.Jp[i + n * j] + M.Jp[j + n * i]);
-            const double K = 0.125 * rr * (M.Kp[i + n * j] + M.Kp[j + n * i]);
-            const double f = M.H[idx] + 2.0 * J - K;
-            M.F[idx] = f;
-            e += M.D[idx] * (M.H[idx] + f);
-        }
-        E = qb_cta_sum(e, red);   // also a barrier: all reads of J', K' are done
-        for (int i = tid; i < nn; i += nt) {
-            M.Jp[i] = 0.0;
-            M.Kp[i] = 0.0;
-        }
-        __syncthreads();
-    }
-    // F' = X^T F X  (W2)
-    qb_cta_gemm(false, false, n, n, n, 1.0, M.F, n, M.X, n, 0.0, M.W1, n);
-    qb_cta_gemm_sym(true, false, n, n, M.X, n, M.W1, n, M.W2, n);
-    if (it > 0 && prm.diis > 1) {
-        // DIIS subspace of (F', e', E) entries (initializeHFcore, HartreeFock.jl:1335-1394):
-        // the entry of this density joins, then either the subspace restarts from the
-        // previous entry (energy rise above resetThreshold) or, when over size, the entry of
-        // highest energy leaves; F' is then extrapolated with the Pulay coefficients.
-        if (tid == 0) {
-            unsigned used_mask = 0;
-            for (int k = 0; k < M.dlen; ++k) used_mask |= 1u << M.dlist[k];
-            int slot = 0;
-            while (used_mask & (1u << slot)) ++slot;
-            s_idx[0] = slot;
-        }
-        __syncthreads();
-        const int slot = s_idx[0];
-        double* Fs = M.Fh + (size_t)slot * nn;
-        double* Es = M.Eh + (size_t)slot * nn;
-        // e' = F' D' - D' F' = X^T (F D S - S D F) X (getEresidual, :1298-1299)
-        qb_cta_gemm(false, false, n, n, n, 1.0, M.W2, n, M.Do, n, 0.0, M.W1, n);
-        for (int idx = tid; idx < nn; idx += nt) {
-            const int i = idx % n, j = idx / n;
-            Es[idx] = M.W1[i + n * j] - M.W1[j + n * i];
-            Fs[idx] = M.W2[idx];
-        }
-        __syncthreads();
-        const int len0 = M.dlen;
-        for (int k = tid >> 5; k <= len0; k += nt >> 5) {   // one warp per Gram-matrix entry
-            const int other = (k < len0) ? M.dlist[k] : slot;
-            const double* Ek = M.Eh + (size_t)other * nn;
-            double dot = 0.0;
-            for (int idx = tid & 31; idx < nn; idx += 32) dot = fma(Es[idx], Ek[idx], dot);
-            dot = qb_group_sum(dot, 32);
-            if ((tid & 31) == 0) {
-                M.B[slot * QB_BATCH_SLOTS + other] = dot;
-                M.B[other * QB_BATCH_SLOTS + slot] = dot;
-            }
-        }
-        __syncthreads();
-        if (tid == 0) {
-            M.dEs[slot] = 0.5 * E;   // per-spin energy of the entry
-            M.dlist[M.dlen++] = slot;
-            const int L = M.dlen;
-            if (L > 2 && M.dEs[M.dlist[L - 1]] - M.dEs[M.dlist[L - 2]] > QB_BATCH_RESET) {
-                M.dlist[0] = M.dlist[L - 2];   // keepOnly! of the second-to-last entry
-                M.dlen = 1;
-            } else if (L > prm.diis) {
-                int pi = 0;
-                for (int k = 1; k < L; ++k)
-                    if (M.dEs[M.dlist[k]] > M.dEs[M.dlist[pi]]) pi = k;
-                for (int k = pi; k + 1 < L; ++k) M.dlist[k] = M.dlist[k + 1];
-                M.dlen = L - 1;
-            }
-            const int m = M.dlen;
-            for (int k = 0; k < m; ++k) s_idx[k] = M.dlist[k];
-            s_ok = m;
-        }
-        __syncthreads();
-        const int m = s_ok;
-        if (tid < 32) {   // Pulay coefficients by warp 0
-            bool ok = true;
-            if (m == 1) {
-                if (tid == 0) s_c[0] = 1.0;
-            } else {
-                ok = qb_diis_coeffs_warp(m, M.B, s_idx, s_c, s_diis);
-            }
-            if (!ok && tid == 0) {   // singular system: extrapolate with the newest entry only
-                for (int k = 0; k < m; ++k) s_c[k] = 0.0;
-                s_c[m - 1] = 1.0;
-            }
-        }
-        __syncthreads();
-        for (int idx = tid; idx < nn; idx += nt) {
-            double f = 0.0;
-            for (int k = 0; k < m; ++k) f = fma(s_c[k], M.Fh[(size_t)s_idx[k] * nn + idx], f);
-            M.W2[idx] = f;
-        }
-        __syncthreads();
-    }
     int used = 0;
     if (prm.eig == 0) {
-        // occupied eigenvectors Y of F' (W1, n x nocc): Householder + bisection + inverse
-        // iteration; D' = Y Y^T (W3) and D = (X Y)(X Y)^T (W2)
         const int k = M.nocc;
         double *Aw = M.W3, *Yw = M.W1;
         for (int i = tid; i < nn; i += nt) Aw[i] = M.W2[i];
@@ -434,61 +329,449 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
         qb_cta_gemm(false, false, n, k, n, 1.0, M.X, n, Yw, n, 0.0, M.W4, n);
         qb_cta_gemm_sym(false, true, n, k, M.W4, n, M.W4, n, M.W2, n);
     } else {
-        // rotate into the previous eigenvectors, A = C'^T F' C' (W3), and diagonalise;
-        // eigenvectors to off(A) <= 1e-12 ||A||: the density they give is exact far below
-        // the 1e-8 density threshold, and the warm start usually needs a single sweep
+        // rotate into the previous eigenvectors, A = C'^T F' C' (W3), and diagonalise
         qb_cta_gemm(false, false, n, n, n, 1.0, M.W2, n, M.Cp, n, 0.0, M.W1, n);
         qb_cta_gemm(true, false, n, n, n, 1.0, M.Cp, n, M.W1, n, 0.0, M.W3, n);
         used = qb_cta_jacobi<QB_BATCH_MAXN>(n, M.W3, M.W1, M.Cp, M.eps, M.wt, M.W2, prm.sweeps, jsm, 1e-24);
         for (int i = tid; i < nn; i += nt) M.Cp[i] = M.W1[i];
         __syncthreads();
-        // D' = C'_occ C'_occ^T (W3); D = X D' X^T (W2)
         qb_cta_gemm(false, true, n, n, M.nocc, 1.0, M.Cp, n, M.Cp, n, 0.0, M.W3, n);
         qb_cta_gemm(false, false, n, n, n, 1.0, M.X, n, M.W3, n, 0.0, M.W1, n);
         qb_cta_gemm(false, true, n, n, n, 1.0, M.W1, n, M.X, n, 0.0, M.W2, n);
     }
-    double dd = 0.0;
-    for (int idx = tid; idx < nn; idx += nt) {
-        const double d = M.W2[idx] - M.D[idx];
-        dd += d * d;
-    }
-    dd = qb_cta_sum(dd, red);
-    const double rms = 2.0 * sqrt(dd) / n;   // RMS change of the total density 2D
+    __syncthreads();
+    return used < 0 ? prm.sweeps : used;
+}
+
+// the next density to digest: D (AO) with its ratio-scaled copy, and D' (orthonormal)
+__device__ void qb_batch_set_density(MolDev& M, const double* Dao, const double* Dorth) {
+    const int n = M.n, nn = n * n, tid = threadIdx.x, nt = blockDim.x;
     for (int idx = tid; idx < nn; idx += nt) {
         const int i = idx % n, j = idx / n;
-        const double d = M.W2[idx];
+        const double d = Dao[idx];
         M.D[idx] = d;
-        M.Dt[idx] = d * r[i] * r[j];
-        M.Do[idx] = M.W3[idx];
+        M.Dt[idx] = d * M.ratio[i] * M.ratio[j];
+        M.Do[idx] = Dorth[idx];
     }
     __syncthreads();
-    if (tid == 0) {
-        M.sweeps += used < 0 ? prm.sweeps : used;   // Jacobi sweeps (0 with the tridiagonal solver)
-        // convergence of the entry of this step (E of D, and D against the density before
-        // it), as runHartreeFockCore compares consecutive steps (HartreeFock.jl:1160-1175)
-        int conv = 0;
-        if (it > 0) {
-            M.dE = E - M.Eprev;
-            if (it >= 2 && fabs(M.dE) <= prm.thr_e && M.rmsD <= prm.thr_d) conv = 1;
-            M.E = E;
-            M.Eprev = E;
+}
+
+__device__ __forceinline__ int qb_stage_len(int method, int diis) {   // max(HFinterMatStoreSizes..., cache size)
+    return method == QB_SCF_DD ? 3 : (diis > 3 ? diis : 3);
+}
+
+// isOscillateConverged (src/Tools.jl:291-315), minimum-seeking, minLen 10, maxRemains 15, on
+// the ring of the last total energies
+__device__ bool qb_osc_converged(const MolDev& M, double tar) {
+    const int len = M.ne;
+    if (len < 10) return false;
+    const int slice = min(15, len / 3 + 1);
+    if (slice < 2) return false;
+    double v[15];
+    for (int k = 0; k < slice; ++k) v[k] = M.Er[(len - slice + k) & 31];
+    for (int i = 1; i < slice; ++i) {   // insertion sort
+        const double t = v[i];
+        int j = i - 1;
+        while (j >= 0 && v[j] > t) {
+            v[j + 1] = v[j];
+            --j;
         }
-        M.rmsD = rms;   // change of the density handed to the next step
-        M.iter = it + 1;
-        const int spent = M.iter0 + M.iter;
-        if (!conv && prm.fallback > 0 && !M.restarted && M.iter >= prm.fallback && spent < prm.max_iter) {
-            // the supplied initial density has not converged: start again from F = H with an
-            // empty DIIS subspace (the next step ignores D and the J'/K' of this iteration)
-            M.iter0 = spent;
-            M.iter = 0;
-            M.dlen = 0;
-            M.restarted = 1;
-        } else if (!conv && spent >= prm.max_iter) {
-            conv = 2;
-        }
-        M.conv = conv;
-        if (!conv) atomicAdd(active, 1);
+        v[j + 1] = t;
     }
+    const int nv = slice / 2 + 1;
+    double mean = 0.0;
+    for (int k = 0; k < nv; ++k) mean += v[k];
+    mean /= nv;
+    double var = 0.0;
+    for (int k = 0; k < nv; ++k) var += (v[k] - mean) * (v[k] - mean);
+    const double sd = nv > 1 ? sqrt(var / (nv - 1)) : 0.0;
+    return sd <= 0.8 * tar && fabs(v[0] - M.Er[(len - 1) & 31]) <= tar;
+}
+
+// start of a method (initializeHFcore, HartreeFock.jl:1335-1360): a DIIS-type method takes
+// the last min(DIISsize, history) entries as its subspace, coefficients 1, 2, ..., m
+__device__ void qb_stage_init(MolDev& M, const StepParams& prm) {
+    M.nstep = 0;
+    M.slen = 0;
+    if (M.stage >= prm.nmethod || prm.method[M.stage] == QB_SCF_DD) return;
+    const int init = min(prm.diis, M.hlen);
+    for (int k = 0; k < init; ++k) {
+        M.slist[k] = M.hlist[M.hlen - init + k];
+        M.c[k] = (double)(k + 1);
+    }
+    M.slen = init;
+}
+
+// One SCF step of one molecule per thread block (blocks ordered by size, largest first),
+// following runHartreeFockCore (src/HartreeFock.jl:1049-1228) method by method: the
+// digested density's Fock matrix either finishes a DD half step (directDiag, :1245-1270) or
+// is a step's entry (C, D, F, E) that joins the history and the DIIS subspace (:1361-1390),
+// is tested for convergence (:1160-1175), oscillation and early termination (:1177-1203),
+// after which the next step of the current method starts.
+__global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev* mols, const int* __restrict__ order,
+                                                                         const StepParams prm, int* active) {
+    __shared__ QbJacobiSmem<QB_BATCH_MAXN> jsm;
+    __shared__ QbEigSmem<QB_BATCH_MAXN> esm;
+    __shared__ double red[33];
+    __shared__ double s_B[QB_BATCH_DIIS * QB_BATCH_DIIS], s_v[QB_BATCH_DIIS];
+    __shared__ int s_idx[QB_BATCH_POOL], s_slot, s_nlive, s_act, s_stale, s_needF;
+    __shared__ double s_diis[QB_BATCH_DIIS + 2][QB_BATCH_DIIS + 3];
+    MolDev& M = mols[order[blockIdx.x]];
+    if (M.conv) return;
+    const int n = M.n, nn = n * n, tid = threadIdx.x, nt = blockDim.x;
+    const double* r = M.ratio;
+    const int it = M.iter;
+    if (it == 0) {
+        // core-Hamiltonian guess (also after a restart): F = H; drop what the digest accumulated
+        for (int i = tid; i < nn; i += nt) {
+            M.F[i] = M.H[i];
+            M.Jp[i] = 0.0;
+            M.Kp[i] = 0.0;
+        }
+        __syncthreads();
+        qb_cta_gemm(false, false, n, n, n, 1.0, M.F, n, M.X, n, 0.0, M.W1, n);
+        qb_cta_gemm_sym(true, false, n, n, M.X, n, M.W1, n, M.W2, n);
+        const int used = qb_batch_density(M, prm, jsm, esm);
+        qb_batch_set_density(M, M.W2, M.W3);
+        if (tid == 0) {
+            M.sweeps += used;
+            M.iter = 1;
+            M.phase = 0;
+            M.steps = 0;
+            M.stage = 0;
+            M.nstep = 0;
+            M.hlen = M.slen = M.ne = M.nde = 0;
+            M.stale = 0;
+            atomicAdd(active, 1);
+        }
+        return;
+    }
+    // F = H + 2J - K of the digested density (libint-convention accumulators, per-function
+    // ratios) and E = tr(D (H + F)) (getE, :339-342, summed over the two equal spins)
+    double e = 0.0;
+    for (int idx = tid; idx < nn; idx += nt) {
+        const int i = idx % n, j = idx / n;
+        const double rr = r[i] * r[j];
+        const double J = 0.25 * rr * (M.Jp[i + n * j] + M.Jp[j + n * i]);
+        const double K = 0.125 * rr * (M.Kp[i + n * j] + M.Kp[j + n * i]);
+        const double f = M.H[idx] + 2.0 * J - K;
+        M.F[idx] = f;
+        e += M.D[idx] * (M.H[idx] + f);
+    }
+    const double E = qb_cta_sum(e, red);   // also a barrier: all reads of J', K' are done
+    for (int i = tid; i < nn; i += nt) {
+        M.Jp[i] = 0.0;
+        M.Kp[i] = 0.0;
+    }
+    __syncthreads();
+    // F' = X^T F X (W2)
+    qb_cta_gemm(false, false, n, n, n, 1.0, M.F, n, M.X, n, 0.0, M.W1, n);
+    qb_cta_gemm_sym(true, false, n, n, M.X, n, M.W1, n, M.W2, n);
+    if (M.phase == 1) {
+        // second half of a DD step: the entry's density from the eigenvectors of F(D damped)
+        const int used = qb_batch_density(M, prm, jsm, esm);
+        qb_batch_set_density(M, M.W2, M.W3);
+        if (tid == 0) {
+            M.sweeps += used;
+            M.phase = 0;
+            M.iter = it + 1;
+            atomicAdd(active, 1);
+        }
+        return;
+    }
+    // ---- the entry (D, F, E) of a step: a free pool slot, its e', the Gram entries
+    if (tid == 0) {
+        unsigned used_mask = 0;
+        for (int k = 0; k < M.hlen; ++k) used_mask |= 1u << M.hlist[k];
+        for (int k = 0; k < M.slen; ++k) used_mask |= 1u << M.slist[k];
+        int slot = 0;
+        while (slot < QB_BATCH_POOL - 1 && (used_mask & (1u << slot))) ++slot;
+        s_slot = slot;
+        int nl = 0;
+        for (int k = 0; k < QB_BATCH_POOL; ++k)
+            if ((used_mask | (1u << slot)) & (1u << k)) s_idx[nl++] = k;
+        s_nlive = nl;
+    }
+    __syncthreads();
+    const int slot = s_slot;
+    double* Fs = M.Fs + (size_t)slot * nn;
+    double* Ds = M.Ds + (size_t)slot * nn;
+    double* Es = M.Es + (size_t)slot * nn;
+    // e' = F' D' - D' F' = X^T (F D S - S D F) X (getEresidual, :1298-1299)
+    qb_cta_gemm(false, false, n, n, n, 1.0, M.W2, n, M.Do, n, 0.0, M.W1, n);
+    double dd = 0.0;
+    const int last = M.hlen > 0 ? M.hlist[M.hlen - 1] : -1;
+    const double* Dlast = last >= 0 ? M.Ds + (size_t)last * nn : nullptr;
+    for (int idx = tid; idx < nn; idx += nt) {
+        const int i = idx % n, j = idx / n;
+        Es[idx] = M.W1[i + n * j] - M.W1[j + n * i];
+        Fs[idx] = M.F[idx];
+        Ds[idx] = M.D[idx];
+        if (Dlast) {
+            const double t = M.D[idx] - Dlast[idx];
+            dd += t * t;
+        }
+    }
+    dd = qb_cta_sum(dd, red);
+    const double rmsD = 2.0 * sqrt(dd) / n;   // RMS change of the total density 2D (rmsOf, src/Tools.jl:588)
+    const int nl = s_nlive;
+    for (int k = tid >> 5; k < 3 * nl; k += nt >> 5) {   // one warp per Gram entry
+        const int o = s_idx[k % nl], kind = k / nl;
+        const double* a = kind == 0 ? Es : (kind == 1 ? Ds : M.Ds + (size_t)o * nn);
+        const double* b = kind == 0 ? M.Es + (size_t)o * nn : (kind == 1 ? M.Fs + (size_t)o * nn : Fs);
+        double dot = 0.0;
+        for (int idx = tid & 31; idx < nn; idx += 32) dot = fma(a[idx], b[idx], dot);
+        dot = qb_group_sum(dot, 32);
+        if ((tid & 31) == 0) {
+            if (kind == 0) {
+                M.Gee[slot * QB_BATCH_POOL + o] = dot;
+                M.Gee[o * QB_BATCH_POOL + slot] = dot;
+            } else if (kind == 1) {
+                M.Gdf[slot * QB_BATCH_POOL + o] = dot;   // <D_slot, F_o>
+            } else {
+                M.Gdf[o * QB_BATCH_POOL + slot] = dot;   // <D_o, F_slot>
+            }
+        }
+    }
+    __syncthreads();
+    // ---- bookkeeping of the step (thread 0), with the RMS(FDS - SDF) test deferred to the
+    // few steps whose other criteria make it matter
+    const bool first = (M.hlen == 0);
+    const int method = prm.method[min(M.stage, prm.nmethod - 1)];
+    const double bp = prm.interval[min(M.stage, prm.nmethod - 1)];
+    const bool endM = M.stage == prm.nmethod - 1;
+    const double fluc = fmax(10 * bp, 1.5e-3), dEosc = fmax(bp, prm.osc);
+    const double dE = first ? 0.0 : E - M.Eprev;
+    if (tid == 0) {
+        int need = 0;
+        if (!first) {
+            if (fabs(dE) <= bp && rmsD <= prm.r2 * bp) need = 1;
+            if (M.nstep > 1 && M.steps > 10 && dE > fluc && prm.osc > 0 && endM) need = 1;
+        }
+        s_needF = need;
+    }
+    __syncthreads();
+    double dF = -1.0;
+    if (s_needF) {   // getErrorNrms (:1230-1237): RMS(F D S - S D F) in the AO basis
+        qb_cta_gemm(false, false, n, n, n, 1.0, M.D, n, M.S, n, 0.0, M.W1, n);
+        qb_cta_gemm(false, false, n, n, n, 1.0, M.F, n, M.W1, n, 0.0, M.W4, n);
+        double ss = 0.0;
+        for (int idx = tid; idx < nn; idx += nt) {
+            const int i = idx % n, j = idx / n;
+            const double t = M.W4[i + n * j] - M.W4[j + n * i];
+            ss += t * t;
+        }
+        dF = sqrt(qb_cta_sum(ss, red)) / n;
+    }
+    if (tid == 0) {
+        M.sE[slot] = 0.5 * E;   // per-spin energy of the entry
+        // the entry joins the subspace of a DIIS-type method when one of its own steps made it
+        if (!first && method != QB_SCF_DD && M.nstep >= 1) {
+            M.slist[M.slen] = slot;
+            M.c[M.slen] = 1.0;
+            const int L = ++M.slen;
+            if (L > 2 && M.sE[M.slist[L - 1]] - M.sE[M.slist[L - 2]] > QB_BATCH_RESET) {
+                M.slist[0] = M.slist[L - 2];   // keepOnly! of the second-to-last entry
+                M.c[0] = M.c[L - 2];
+                M.slen = 1;
+            } else if (L > prm.diis) {
+                int pi = 0;
+                for (int k = 1; k < L; ++k)
+                    if (M.sE[M.slist[k]] > M.sE[M.slist[pi]]) pi = k;
+                for (int k = pi; k + 1 < L; ++k) {
+                    M.slist[k] = M.slist[k + 1];
+                    M.c[k] = M.c[k + 1];
+                }
+                M.slen = L - 1;
+            }
+        }
+        // history (updateHFtempInfo!, :463-477), truncated to the method's memory length
+        const int len = qb_stage_len(method, prm.diis);
+        while (M.hlen >= len) {
+            for (int k = 0; k + 1 < M.hlen; ++k) M.hlist[k] = M.hlist[k + 1];
+            --M.hlen;
+        }
+        M.hlist[M.hlen++] = slot;
+        M.Er[M.ne & 31] = E;
+        ++M.ne;
+        M.stale = 0;
+        bool done = false;
+        if (first) {
+            M.Eprev = E;
+            M.dE = 0.0;
+            M.rmsD = 0.0;
+            qb_stage_init(M, prm);
+        } else {
+            M.dE = dE;
+            M.rmsD = rmsD;
+            M.dF = dF;
+            M.dEr[M.nde & 3] = dE;
+            ++M.nde;
+            M.Eprev = E;
+            // convergence of the method (:1168-1175): |dE| and RMS(dD) gated by RMS(FDS - SDF)
+            // (a failed gate zeroes both thresholds, which dE = dD = 0 still meets)
+            bool conv = (fabs(dE) <= bp && rmsD <= prm.r2 * bp && dF <= prm.r1 * bp) || (dE == 0.0 && rmsD == 0.0);
+            bool stop = false;
+            if (!conv && M.nstep > 1 && M.steps > 10 && dE > fluc) {
+                bool isOsc = false;
+                if (prm.osc > 0) {
+                    isOsc = qb_osc_converged(M, 10 * dEosc);
+                    if (isOsc && fabs(dE) <= dEosc &&
+                        (endM ? (dF >= 0 && dF <= prm.r1 * dEosc && rmsD <= prm.r2 * dEosc) : true))
+                        conv = true;   // converged to an oscillation
+                }
+                if (!conv && prm.early_stop && !isOsc) {
+                    bool raising = M.nde >= 4;
+                    for (int j = 0; j < 4 && raising; ++j)
+                        if (!(M.dEr[(M.nde - 1 - j) & 3] > 10 * fluc)) raising = false;
+                    if (raising) {   // terminateSCF!: roll the last steps back, end the method
+                        const int rb = min(4, max(M.hlen - 1, 0));
+                        M.hlen -= rb;
+                        M.ne -= rb;
+                        M.steps -= rb;
+                        M.stale = rb > 0;
+                        M.Eprev = M.Er[(M.ne - 1) & 31];
+                        stop = true;
+                    }
+                }
+            }
+            if (conv || stop) {
+                if (endM) {
+                    M.conv = conv ? 1 : 2;
+                    done = true;
+                } else {
+                    ++M.stage;
+                    qb_stage_init(M, prm);
+                }
+            }
+        }
+        if (!done && M.iter0 + M.steps >= prm.max_iter) {   // i < maxStep || break (:1144)
+            M.conv = 2;
+            done = true;
+        }
+        if (!done && prm.fallback > 0 && !M.restarted && M.steps >= prm.fallback && M.iter0 + M.steps < prm.max_iter) {
+            // the supplied initial density has not converged: start again from F = H
+            M.iter0 += M.steps;
+            M.iter = 0;
+            M.restarted = 1;
+            done = true;   // the next call makes the core-Hamiltonian guess
+            atomicAdd(active, 1);
+        }
+        s_act = done ? 0 : 1;
+        s_stale = M.stale;
+        if (!done) {
+            ++M.steps;
+            ++M.nstep;
+        }
+    }
+    __syncthreads();
+    if (!s_act) return;   // stopped (the finish kernel takes the history's last entry) or restarting
+    const int meth = prm.method[M.stage];
+    const int lst = M.hlist[M.hlen - 1];
+    if (s_stale) {
+        // after a rollback the step starts from an earlier entry: its F' (W2), D (AO) and D' (Do)
+        qb_cta_gemm(false, false, n, n, n, 1.0, M.Fs + (size_t)lst * nn, n, M.X, n, 0.0, M.W1, n);
+        qb_cta_gemm_sym(true, false, n, n, M.X, n, M.W1, n, M.W2, n);
+        qb_cta_gemm(false, false, n, n, n, 1.0, M.Sh, n, M.Ds + (size_t)lst * nn, n, 0.0, M.W1, n);
+        qb_cta_gemm(false, true, n, n, n, 1.0, M.W1, n, M.Sh, n, 0.0, M.Do, n);
+        for (int i = tid; i < nn; i += nt) M.D[i] = M.Ds[(size_t)lst * nn + i];
+        __syncthreads();
+    }
+    int used = 0;
+    if (meth == QB_SCF_DD) {
+        // directDiag: D_damped = (1 - lambda) D(eigenvectors of F_last) + lambda D_last, then its Fock matrix
+        for (int i = tid; i < nn; i += nt) M.W5[i] = M.Do[i];   // D'_last
+        __syncthreads();
+        used = qb_batch_density(M, prm, jsm, esm);
+        const double lam = prm.damp;
+        for (int idx = tid; idx < nn; idx += nt) {
+            const int i = idx % n, j = idx / n;
+            const double d = (1.0 - lam) * M.W2[idx] + lam * M.D[idx];
+            M.D[idx] = d;
+            M.Dt[idx] = d * r[i] * r[j];
+            M.Do[idx] = (1.0 - lam) * M.W3[idx] + lam * M.W5[idx];
+        }
+        __syncthreads();
+        if (tid == 0) M.phase = 1;
+    } else {
+        // DIIS / EDIIS / ADIIS (DIIScore :1301-1315, EDIIScore :1273-1285, ADIIScore :1287-1296)
+        const int m = M.slen;
+        if (tid == 0) {
+            for (int k = 0; k < m; ++k) s_idx[k] = M.slist[k];
+        }
+        __syncthreads();
+        const int L = m - 1;
+        for (int q = tid; q < m * m; q += nt) {
+            const int i = q % m, j = q / m;
+            const int a = s_idx[i], b = s_idx[j], l = s_idx[L];
+            double bv;
+            if (meth == QB_SCF_DIIS) {
+                bv = M.Gee[a * QB_BATCH_POOL + b];
+            } else if (meth == QB_SCF_EDIIS) {
+                bv = -(M.Gdf[a * QB_BATCH_POOL + a] - M.Gdf[a * QB_BATCH_POOL + b] - M.Gdf[b * QB_BATCH_POOL + a] +
+                       M.Gdf[b * QB_BATCH_POOL + b]);
+            } else {
+                bv = M.Gdf[a * QB_BATCH_POOL + b] - M.Gdf[a * QB_BATCH_POOL + l] - M.Gdf[l * QB_BATCH_POOL + b] +
+                     M.Gdf[l * QB_BATCH_POOL + l];
+            }
+            s_B[i + m * j] = bv;
+            if (j == 0) {
+                s_v[i] = meth == QB_SCF_DIIS ? 0.0
+                                             : (meth == QB_SCF_EDIIS ? M.sE[a]
+                                                                     : M.Gdf[a * QB_BATCH_POOL + l] - M.Gdf[l * QB_BATCH_POOL + l]);
+            }
+        }
+        __syncthreads();
+        const int sv = prm.solver[M.stage];
+        if (m == 1) {
+            if (tid == 0) M.c[0] = 1.0;
+        } else if (sv == QB_DIIS_LCM && meth == QB_SCF_DIIS) {
+            if (tid < 32) {
+                const bool ok = qb_diis_coeffs_warp(m, M.Gee, s_idx, M.c, s_diis);
+                if (!ok && tid == 0) {   // singular system: extrapolate with the newest entry only
+                    for (int k = 0; k < m; ++k) M.c[k] = 0.0;
+                    M.c[m - 1] = 1.0;
+                }
+            }
+        } else if (tid == 0) {
+            if (sv == QB_DIIS_LCM) qb_cm_solve(*M.dw, m, meth != QB_SCF_DIIS, s_B, m, s_v, M.c);
+            else qb_diis_iterative_solve(*M.dw, sv, meth != QB_SCF_DIIS, m, s_B, m, s_v, M.c);
+        }
+        __syncthreads();
+        // F = sum_k c_k F_k (AO) -> F' = X^T F X
+        for (int idx = tid; idx < nn; idx += nt) {
+            double f = 0.0;
+            for (int k = 0; k < m; ++k) f = fma(M.c[k], M.Fs[(size_t)s_idx[k] * nn + idx], f);
+            M.W3[idx] = f;
+        }
+        __syncthreads();
+        qb_cta_gemm(false, false, n, n, n, 1.0, M.W3, n, M.X, n, 0.0, M.W1, n);
+        qb_cta_gemm_sym(true, false, n, n, M.X, n, M.W1, n, M.W2, n);
+        used = qb_batch_density(M, prm, jsm, esm);
+        qb_batch_set_density(M, M.W2, M.W3);
+    }
+    if (tid == 0) {
+        M.sweeps += used;
+        M.iter = it + 1;
+        atomicAdd(active, 1);
+    }
+}
+
+// After the iterations: each molecule's result is its history's last entry.
+__global__ void qb_batch_finish_kernel(MolDev* mols) {
+    MolDev& M = mols[blockIdx.x];
+    if (M.conv == 3 || M.hlen == 0) return;
+    const int nn = M.n * M.n;
+    const double* Dfin = M.Ds + (size_t)M.hlist[M.hlen - 1] * nn;
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) M.D[i] = Dfin[i];
+    if (threadIdx.x == 0) M.E = 2.0 * M.sE[M.hlist[M.hlen - 1]];
+}
+
+// Loop condition of the SCF graph: another pass while some molecule iterates, at most
+// `cap` passes in all.
+__global__ void qb_batch_cond_kernel(cudaGraphConditionalHandle handle, const int* active, int* passes, int cap) {
+    const int p = ++(*passes);
+    cudaGraphSetConditional(handle, (*active > 0 && p < cap) ? 1u : 0u);
 }
 
 template <int LA, int LB, int LC, int LD>
@@ -535,6 +818,17 @@ extern "C" void qb_batch_config_default(qb_batch_config* cfg) {
     cfg->jacobi_sweeps = 0;
     cfg->eigensolver = 0;
     cfg->fallback_iter = 0;
+    cfg->nmethod = 0;   // one DIIS method at conv_energy with exact (Lagrange-multiplier) coefficients
+    for (int l = 0; l < 8; ++l) {
+        cfg->method[l] = QB_SCF_DIIS;
+        cfg->interval[l] = 0.0;
+        cfg->solver[l] = QB_DIIS_LBFGS;
+    }
+    cfg->secondary_ratio[0] = 1000.0;
+    cfg->secondary_ratio[1] = 1000.0;
+    cfg->oscillate_threshold = 5e-6;
+    cfg->early_stop = 1;
+    cfg->damp_strength = 0.75;
 }
 
 int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nnuc, const double* Z,
@@ -548,6 +842,16 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
         cfg.fallback_iter < 0 ||
         !(cfg.schwarz >= 0.0) || !(cfg.conv_energy > 0.0) || !(cfg.conv_density > 0.0))
         return qb_set_error(ctx, QB_ERR_DOMAIN, "bad batched SCF configuration");
+    if (cfg.nmethod < 0 || cfg.nmethod > 8) return qb_set_error(ctx, QB_ERR_ARG, "nmethod must be 0..8");
+    for (int l = 0; l < cfg.nmethod; ++l) {
+        if (cfg.method[l] < QB_SCF_DD || cfg.method[l] > QB_SCF_ADIIS || !(cfg.interval[l] >= 0.0))
+            return qb_set_error(ctx, QB_ERR_ARG, "bad SCF method or threshold");
+        if (cfg.solver[l] < QB_DIIS_LBFGS || cfg.solver[l] > QB_DIIS_LCM)
+            return qb_set_error(ctx, QB_ERR_ARG, "unknown DIIS coefficient solver");
+    }
+    if (cfg.nmethod > 0 && (!(cfg.damp_strength >= 0.0 && cfg.damp_strength <= 1.0) ||
+                            !(cfg.secondary_ratio[0] > 0.0) || !(cfg.secondary_ratio[1] > 0.0)))
+        return qb_set_error(ctx, QB_ERR_DOMAIN, "bad damping or secondary convergence ratio");
     cudaStream_t s = ctx->stream;
     // ---- concatenate the bases, detect shells per molecule
     std::vector<int> fo(nmol + 1, 0), nf(nmol), nuc0(nmol + 1, 0);
@@ -632,26 +936,32 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
         vo[m + 1] = vo[m] + nf[m];
     }
     const long long NN = mo[nmol];
-    const int nmat = 16 + 2 * QB_BATCH_SLOTS;
-    DevArray<double> d_mats, d_vecs, d_B;
+    const int nbase = 17;   // S, H, X, S^1/2, F, D, Dt, D', J', K', C', 6 work matrices
+    const int nmat = nbase + 3 * QB_BATCH_POOL;
+    DevArray<double> d_mats, d_vecs, d_G;
+    DevArray<QbDiisWork> d_dw;
     QB_CUDA(ctx, d_mats.ensure((size_t)nmat * NN));
     QB_CUDA(ctx, d_vecs.ensure(2 * (size_t)vo[nmol]));
-    QB_CUDA(ctx, d_B.ensure((size_t)nmol * QB_BATCH_SLOTS * QB_BATCH_SLOTS));
-    QB_CUDA(ctx, cudaMemsetAsync(d_B.p, 0, (size_t)nmol * QB_BATCH_SLOTS * QB_BATCH_SLOTS * sizeof(double), s));
+    QB_CUDA(ctx, d_G.ensure((size_t)nmol * 2 * QB_BATCH_POOL * QB_BATCH_POOL));
+    QB_CUDA(ctx, d_dw.ensure(nmol));
+    QB_CUDA(ctx, cudaMemsetAsync(d_G.p, 0, (size_t)nmol * 2 * QB_BATCH_POOL * QB_BATCH_POOL * sizeof(double), s));
     std::vector<MolDev> hm(nmol);
     for (int m = 0; m < nmol; ++m) {
         MolDev& M = hm[m];
         std::memset(&M, 0, sizeof(M));
         M.n = nf[m];
         M.nocc = nocc[m];
-        double* mat[16];
-        for (int k = 0; k < 16; ++k) mat[k] = d_mats.p + (size_t)k * NN + mo[m];
+        double* mat[17];
+        for (int k = 0; k < 17; ++k) mat[k] = d_mats.p + (size_t)k * NN + mo[m];
         M.S = mat[0]; M.H = mat[1]; M.X = mat[2]; M.F = mat[3]; M.D = mat[4]; M.Dt = mat[5]; M.Do = mat[6];
         M.Jp = mat[7]; M.Kp = mat[8]; M.Cp = mat[9]; M.W1 = mat[10]; M.W2 = mat[11]; M.W3 = mat[12];
-        M.W4 = mat[13]; M.W5 = mat[14]; M.W6 = mat[15];
-        M.Fh = d_mats.p + 16 * (size_t)NN + (size_t)QB_BATCH_SLOTS * mo[m];
-        M.Eh = d_mats.p + (16 + QB_BATCH_SLOTS) * (size_t)NN + (size_t)QB_BATCH_SLOTS * mo[m];
-        M.B = d_B.p + (size_t)m * QB_BATCH_SLOTS * QB_BATCH_SLOTS;
+        M.W4 = mat[13]; M.W5 = mat[14]; M.W6 = mat[15]; M.Sh = mat[16];
+        M.Fs = d_mats.p + (size_t)nbase * NN + (size_t)QB_BATCH_POOL * mo[m];
+        M.Ds = d_mats.p + (size_t)(nbase + QB_BATCH_POOL) * NN + (size_t)QB_BATCH_POOL * mo[m];
+        M.Es = d_mats.p + (size_t)(nbase + 2 * QB_BATCH_POOL) * NN + (size_t)QB_BATCH_POOL * mo[m];
+        M.Gee = d_G.p + (size_t)m * 2 * QB_BATCH_POOL * QB_BATCH_POOL;
+        M.Gdf = M.Gee + QB_BATCH_POOL * QB_BATCH_POOL;
+        M.dw = d_dw.p + m;
         M.eps = d_vecs.p + vo[m];
         M.wt = d_vecs.p + vo[nmol] + vo[m];
         M.ratio = d_ratio.p + fo[m];
@@ -892,40 +1202,116 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     QB_CUDA(ctx, d_order.ensure(nmol));
     QB_CUDA(ctx, cudaMemcpyAsync(d_order.p, order.data(), nmol * sizeof(int), cudaMemcpyHostToDevice, s));
     QB_CUDA(ctx, cudaStreamSynchronize(s));
-    const StepParams prm{cfg.conv_energy, cfg.conv_density, cfg.max_iter, cfg.diis_size,
-                         cfg.jacobi_sweeps > 0 ? std::min(cfg.jacobi_sweeps, 60) : 60, cfg.eigensolver ? 1 : 0,
-                         cfg.initial_density && cfg.fallback_iter > 0 ? cfg.fallback_iter : 0};
+    StepParams prm;
+    std::memset(&prm, 0, sizeof(prm));
+    if (cfg.nmethod == 0) {   // SCFconfig((:DIIS,), (conv_energy,), Dict(1=>[:solver=>:LCM])), RMS(dD) <= conv_density
+        prm.nmethod = 1;
+        prm.method[0] = QB_SCF_DIIS;
+        prm.interval[0] = cfg.conv_energy;
+        prm.solver[0] = QB_DIIS_LCM;
+        prm.r1 = 1e6;
+        prm.r2 = cfg.conv_density / cfg.conv_energy;
+        prm.osc = 5e-6;
+        prm.early_stop = 1;
+        prm.damp = 0.75;
+    } else {
+        prm.nmethod = cfg.nmethod;
+        for (int l = 0; l < cfg.nmethod; ++l) {
+            prm.method[l] = cfg.method[l];
+            prm.interval[l] = cfg.interval[l];
+            prm.solver[l] = cfg.solver[l];
+        }
+        prm.r1 = cfg.secondary_ratio[0];
+        prm.r2 = cfg.secondary_ratio[1];
+        prm.osc = cfg.oscillate_threshold;
+        prm.early_stop = cfg.early_stop;
+        prm.damp = cfg.damp_strength;
+    }
+    prm.max_iter = cfg.max_iter;
+    prm.diis = std::max(2, cfg.diis_size);
+    prm.sweeps = cfg.jacobi_sweeps > 0 ? std::min(cfg.jacobi_sweeps, 60) : 60;
+    prm.eig = cfg.eigensolver ? 1 : 0;
+    prm.fallback = cfg.initial_density && cfg.fallback_iter > 0 ? cfg.fallback_iter : 0;
     int* d_active = d_counters.p + 1;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    QB_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < cfg.iters_per_graph; ++k) {
-        cudaMemsetAsync(d_active, 0, sizeof(int), s);
+    DevArray<int> d_passes;
+    QB_CUDA(ctx, d_passes.ensure(1));
+    QB_CUDA(ctx, cudaMemsetAsync(d_passes.p, 0, sizeof(int), s));
+    // one SCF pass: the digest of every iterating molecule's density, then its step
+    auto pass = [&](cudaStream_t st) {
+        cudaMemsetAsync(d_active, 0, sizeof(int), st);
         for (int c = 0; c < QB_BATCH_NCLASS; ++c) {
             const int nch = (int)(chunk_at[c + 1] - chunk_at[c]);
             if (nch == 0) continue;
-            kClasses[c].digest(work[c], d_chunks.p + chunk_at[c], d_eri.p + eri_at[c], d_mols.p, nch, s);
+            kClasses[c].digest(work[c], d_chunks.p + chunk_at[c], d_eri.p + eri_at[c], d_mols.p, nch, st);
         }
-        qb_batch_step_kernel<<<nmol, QB_BATCH_THREADS, 0, s>>>(d_mols.p, d_order.p, prm, d_active);
-    }
-    const cudaError_t cap = cudaStreamEndCapture(s, &graph);
-    QB_CUDA(ctx, cap);
-    QB_CUDA(ctx, cudaGraphInstantiate(&exec, graph, 0));
-    int launches = 0, active = nmol;
-    const int max_launch = (cfg.max_iter + cfg.iters_per_graph - 1) / cfg.iters_per_graph + 1;
+        qb_batch_step_kernel<<<nmol, QB_BATCH_THREADS, 0, st>>>(d_mols.p, d_order.p, prm, d_active);
+    };
+    // every molecule needs at most 2 passes per SCF step, plus the guesses (a restart doubles them)
+    const int cap = 2 * cfg.max_iter + 8;
+    int launches = 0;
     int rc = QB_OK;
-    while (active > 0 && launches < max_launch) {
-        rc = qb_cuda_check(ctx, cudaGraphLaunch(exec, s), "graph launch");
-        if (rc != QB_OK) break;
-        ++launches;
-        rc = qb_cuda_check(ctx, cudaMemcpyAsync(&active, d_active, sizeof(int), cudaMemcpyDeviceToHost, s),
-                           "active count");
-        if (rc == QB_OK) rc = qb_cuda_check(ctx, cudaStreamSynchronize(s), "SCF graph");
-        if (rc != QB_OK) break;
+    {
+        // the whole iteration in one launch: a graph whose conditional while-node repeats the
+        // pass until no molecule iterates (or `cap` passes)
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        cudaGraphConditionalHandle handle;
+        bool ok = cudaGraphCreate(&graph, 0) == cudaSuccess &&
+                  cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        cudaGraphNode_t node;
+        if (ok) {
+            cp.conditional.handle = handle;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            ok = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp) == cudaSuccess;
+        }
+        if (ok) {
+            ok = cudaStreamBeginCaptureToGraph(s, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+            if (ok) {
+                pass(s);
+                qb_batch_cond_kernel<<<1, 1, 0, s>>>(handle, d_active, d_passes.p, cap);
+                cudaGraph_t body = nullptr;
+                ok = cudaStreamEndCapture(s, &body) == cudaSuccess;
+            }
+        }
+        if (ok) ok = cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+        if (ok) {
+            rc = qb_cuda_check(ctx, cudaGraphLaunch(exec, s), "SCF graph launch");
+            launches = 1;
+            if (rc == QB_OK) rc = qb_cuda_check(ctx, cudaStreamSynchronize(s), "SCF graph");
+        } else {
+            cudaGetLastError();   // conditional nodes unavailable: fall back to host-driven launches
+        }
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (!ok && rc == QB_OK) {
+            // several passes per captured graph, the host checking between launches
+            cudaGraph_t g2 = nullptr;
+            cudaGraphExec_t e2 = nullptr;
+            QB_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            for (int k = 0; k < cfg.iters_per_graph; ++k) pass(s);
+            QB_CUDA(ctx, cudaStreamEndCapture(s, &g2));
+            QB_CUDA(ctx, cudaGraphInstantiate(&e2, g2, 0));
+            int active = nmol;
+            const int max_launch = (cap + cfg.iters_per_graph - 1) / cfg.iters_per_graph;
+            while (active > 0 && launches < max_launch) {
+                rc = qb_cuda_check(ctx, cudaGraphLaunch(e2, s), "graph launch");
+                if (rc != QB_OK) break;
+                ++launches;
+                rc = qb_cuda_check(ctx, cudaMemcpyAsync(&active, d_active, sizeof(int), cudaMemcpyDeviceToHost, s),
+                                   "active count");
+                if (rc == QB_OK) rc = qb_cuda_check(ctx, cudaStreamSynchronize(s), "SCF graph");
+                if (rc != QB_OK) break;
+            }
+            cudaGraphExecDestroy(e2);
+            cudaGraphDestroy(g2);
+        }
     }
-    cudaGraphExecDestroy(exec);
-    cudaGraphDestroy(graph);
     QB_TRY(rc);
+    qb_batch_finish_kernel<<<nmol, 256, 0, s>>>(d_mols.p);
+    QB_CUDA(ctx, cudaGetLastError());
     QB_CUDA(ctx, cudaEventRecord(ev2, s));
     QB_CUDA(ctx, cudaMemcpyAsync(hm.data(), d_mols.p, nmol * sizeof(MolDev), cudaMemcpyDeviceToHost, s));
     if (res->density)
@@ -951,7 +1337,7 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     int failed = 0;
     for (int m = 0; m < nmol; ++m) {
         if (res->energy) res->energy[m] = hm[m].E;
-        if (res->iterations) res->iterations[m] = hm[m].iter0 + hm[m].iter;
+        if (res->iterations) res->iterations[m] = hm[m].iter0 + hm[m].steps;
         if (res->restarted) res->restarted[m] = hm[m].restarted;
         if (res->converged) res->converged[m] = hm[m].conv == 1 ? 1 : 0;
         if (res->jacobi_sweeps) res->jacobi_sweeps[m] = hm[m].sweeps;

@@ -223,106 +223,13 @@ void qb_lincomb(cudaStream_t s, long long len, int m, const double* const* mats,
 }
 
 // ---------------------------------------------------------------------------
-// DIIS coefficient problem (CMsolver!, HartreeFock.jl:1445-1477): solve
-// [B 1; 1 0][c; l] = [-v; 1]; if `convex` and some c < 0, try the subsystems
-// with index subsets removed (by increasing size, smallest |c| first) until a
-// non-negative solution appears; a singular bordered matrix gets B += 4e-13 I.
-// One thread; m <= 16.  Bounded: at most 64 perturbation rounds.
+// DIIS coefficient problem: the Lagrange-multiplier solver (qb_cm_solve, CMsolver!,
+// HartreeFock.jl:1445-1477) or the iterative ones (qb_diis_iterative_solve), one thread,
+// state in the caller's QbDiisWork.
 #define QB_DIIS_MAX 16
-__device__ double lu_solve_dev(int n, double* A, double* b) {   // A n x n col-major, in place; returns det
-    double det = 1.0;
-    for (int k = 0; k < n; ++k) {
-        int p = k;
-        for (int i = k + 1; i < n; ++i)
-            if (fabs(A[i + n * k]) > fabs(A[p + n * k])) p = i;
-        if (A[p + n * k] == 0.0) return 0.0;
-        if (p != k) {
-            for (int j = 0; j < n; ++j) { const double t = A[k + n * j]; A[k + n * j] = A[p + n * j]; A[p + n * j] = t; }
-            const double t = b[k]; b[k] = b[p]; b[p] = t;
-            det = -det;
-        }
-        const double pv = A[k + n * k];
-        det *= pv;
-        for (int i = k + 1; i < n; ++i) {
-            const double f = A[i + n * k] / pv;
-            A[i + n * k] = f;
-            for (int j = k + 1; j < n; ++j) A[i + n * j] -= f * A[k + n * j];
-            b[i] -= f * b[k];
-        }
-    }
-    for (int i = n - 1; i >= 0; --i) {
-        double s = b[i];
-        for (int j = i + 1; j < n; ++j) s -= A[i + n * j] * b[j];
-        b[i] = s / A[i + n * i];
-    }
-    return det;
-}
-
-__global__ void qb_diis_kernel(int m, int convex, const double* Bin, const double* v, double* c, int* status) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const int M = m + 1;
-    double B[QB_DIIS_MAX * QB_DIIS_MAX];
-    double A[(QB_DIIS_MAX + 1) * (QB_DIIS_MAX + 1)], W[(QB_DIIS_MAX + 1) * (QB_DIIS_MAX + 1)];
-    double b[QB_DIIS_MAX + 1], x[QB_DIIS_MAX + 1];
-    for (int i = 0; i < m * m; ++i) B[i] = Bin[i];
-    for (int round = 0; round < 64; ++round) {
-        for (int guard = 0; guard < 64; ++guard) {
-            for (int j = 0; j < M; ++j)
-                for (int i = 0; i < M; ++i)
-                    A[i + M * j] = (i < m && j < m) ? B[i + m * j] : ((i == m && j == m) ? 0.0 : 1.0);
-            for (int i = 0; i < M * M; ++i) W[i] = A[i];
-            for (int i = 0; i < M; ++i) x[i] = 0.0;
-            if (lu_solve_dev(M, W, x) != 0.0) break;
-            for (int i = 0; i < m; ++i) B[i + m * i] += 4e-13;
-        }
-        for (int i = 0; i < m; ++i) b[i] = -v[i];
-        b[m] = 1.0;
-        for (int i = 0; i < M * M; ++i) W[i] = A[i];
-        for (int i = 0; i < M; ++i) x[i] = b[i];
-        lu_solve_dev(M, W, x);
-        bool neg = false;
-        for (int i = 0; i < m; ++i) { c[i] = x[i]; neg |= x[i] < 0.0; }
-        if (!convex || !neg) return;
-        int perm[QB_DIIS_MAX];
-        for (int i = 0; i < m; ++i) perm[i] = i;
-        for (int i = 1; i < m; ++i) {   // stable insertion sort by |c|
-            const int t = perm[i];
-            int j = i - 1;
-            while (j >= 0 && fabs(c[perm[j]]) > fabs(c[t])) { perm[j + 1] = perm[j]; --j; }
-            perm[j + 1] = t;
-        }
-        for (int sz = 1; sz <= m; ++sz) {
-            int comb[QB_DIIS_MAX];
-            for (int t = 0; t < sz; ++t) comb[t] = t;
-            while (true) {
-                bool drop[QB_DIIS_MAX + 1];
-                for (int i = 0; i <= m; ++i) drop[i] = false;
-                for (int t = 0; t < sz; ++t) drop[perm[comb[t]]] = true;
-                int keep[QB_DIIS_MAX + 1], k = 0;
-                for (int i = 0; i <= m; ++i)
-                    if (!drop[i]) keep[k++] = i;
-                for (int jj = 0; jj < k; ++jj) {
-                    x[jj] = b[keep[jj]];
-                    for (int ii = 0; ii < k; ++ii) W[ii + k * jj] = A[keep[ii] + M * keep[jj]];
-                }
-                if (lu_solve_dev(k, W, x) != 0.0) {
-                    bool bad = false;
-                    double cl[QB_DIIS_MAX];
-                    for (int i = 0; i < m; ++i) cl[i] = 0.0;
-                    for (int jj = 0; jj < k - 1; ++jj) cl[keep[jj]] = x[jj];
-                    for (int i = 0; i < m; ++i) { c[i] = cl[i]; bad |= cl[i] < 0.0; }
-                    if (!bad) return;
-                }
-                int pos = sz - 1;
-                while (pos >= 0 && comb[pos] == m - sz + pos) --pos;
-                if (pos < 0) break;
-                ++comb[pos];
-                for (int t = pos + 1; t < sz; ++t) comb[t] = comb[t - 1] + 1;
-            }
-        }
-        for (int i = 0; i < m; ++i) B[i + m * i] += 4e-13;
-    }
-    atomicOr(status, 4);
+__global__ void qb_diis_cm_kernel(int m, int convex, const double* B, const double* v, double* c, QbDiisWork* work,
+                                  int* status) {
+    if (threadIdx.x == 0 && blockIdx.x == 0 && !qb_cm_solve(*work, m, convex, B, m, v, c)) atomicOr(status, 4);
 }
 
 // L-BFGS-B / SPG solve by one thread (qb_diis_solvers.cuh); c holds the starting point.
@@ -334,11 +241,8 @@ __global__ void qb_diis_iter_kernel(int solver, int convex, int m, const double*
 int qb_diis_solve(cudaStream_t s, int m, int convex, int solver, const double* B, const double* v, double* c,
                   QbDiisWork* work, int* status) {
     if (m < 1 || m > QB_DIIS_MAX) return -1;
-    if (solver == QB_DIIS_LCM) {
-        qb_diis_kernel<<<1, 32, 0, s>>>(m, convex, B, v, c, status);
-    } else {
-        if (!work || m > QB_DS_N) return -1;
-        qb_diis_iter_kernel<<<1, 32, 0, s>>>(solver, convex, m, B, v, c, work);
-    }
+    if (!work || m > QB_DS_N) return -1;
+    if (solver == QB_DIIS_LCM) qb_diis_cm_kernel<<<1, 32, 0, s>>>(m, convex, B, v, c, work, status);
+    else qb_diis_iter_kernel<<<1, 32, 0, s>>>(solver, convex, m, B, v, c, work);
     return 0;
 }

@@ -10,7 +10,7 @@
 //   QB_DIIS_SPGB                  SPGBsolver! (:1432-1443): SPGBox.jl 0.7.2, the
 //                                 nonmonotone spectral projected gradient (memory 20,
 //                                 eps = 1e-15);
-//   QB_DIIS_LCM                   CMsolver! (:1445-1477), kept in linalg.cu.
+//   QB_DIIS_LCM                   CMsolver! (:1445-1477), qb_cm_solve below.
 // L-BFGS-B is the method of Byrd, Lu, Nocedal & Zhu (SIAM J. Sci. Comput. 16, 1995) with
 // the stopping and memory-refresh rules of Zhu et al. (ACM TOMS Algorithm 778, 1997), the
 // projected subspace step of Morales & Nocedal (ACM TOMS 38, 2011) and the line search of
@@ -37,6 +37,8 @@ struct QbDiisWork {
     double x[QB_DS_N], g[QB_DS_N], z[QB_DS_N], d[QB_DS_N], r[QB_DS_N], xs[QB_DS_N], gs[QB_DS_N], xp[QB_DS_N];
     double cw[2 * QB_DS_M], p[2 * QB_DS_M], vv[2 * QB_DS_M], wbp[2 * QB_DS_M], wv[2 * QB_DS_M];
     double tb[QB_DS_N], fprev[20];
+    double cmB[QB_DS_N * QB_DS_N], cmA[(QB_DS_N + 1) * (QB_DS_N + 1)], cmW[(QB_DS_N + 1) * (QB_DS_N + 1)];
+    double cmb[QB_DS_N + 1], cmx[QB_DS_N + 1];
     int ord[QB_DS_N], where[QB_DS_N], freel[QB_DS_N], actl[QB_DS_N];
     int nfree, nact;
     int iters;   // solver iterations of the last solve (diagnostics)
@@ -871,7 +873,120 @@ __device__ inline int spg(QbDiisWork& w, int n, bool bounded) {
     return 1;
 }
 
+// LU with partial pivoting of the leading n x n block of A (column-major, leading dimension
+// n), solving A x = b in place of b; returns the determinant (0 when a pivot vanishes).
+__device__ inline double lu_solve(int n, double* A, double* b) {
+    double det = 1.0;
+    for (int k = 0; k < n; ++k) {
+        int p = k;
+        for (int i = k + 1; i < n; ++i)
+            if (fabs(A[i + n * k]) > fabs(A[p + n * k])) p = i;
+        if (A[p + n * k] == 0.0) return 0.0;
+        if (p != k) {
+            for (int j = 0; j < n; ++j) {
+                const double t = A[k + n * j];
+                A[k + n * j] = A[p + n * j];
+                A[p + n * j] = t;
+            }
+            const double t = b[k];
+            b[k] = b[p];
+            b[p] = t;
+            det = -det;
+        }
+        const double pv = A[k + n * k];
+        det *= pv;
+        for (int i = k + 1; i < n; ++i) {
+            const double f = A[i + n * k] / pv;
+            A[i + n * k] = f;
+            for (int j = k + 1; j < n; ++j) A[i + n * j] -= f * A[k + n * j];
+            b[i] -= f * b[k];
+        }
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        double t = b[i];
+        for (int j = i + 1; j < n; ++j) t -= A[i + n * j] * b[j];
+        b[i] = t / A[i + n * i];
+    }
+    return det;
+}
+
 }  // namespace qbds
+
+// CMsolver! (HartreeFock.jl:1445-1477) by one thread: solve [B 1; 1 0][c; l] = [-v; 1]; if
+// `convex` and some c < 0, try the subsystems with index subsets removed (by increasing
+// size, smallest |c| first) until a non-negative solution appears; a singular bordered
+// matrix gets B += 4e-13 I (1000 getAtolVal).  B is m x m with leading dimension ldb, m <= 16.
+// Bounded: at most 64 perturbation rounds; returns false if they run out (c then holds the
+// last candidate).
+static __device__ __noinline__ bool qb_cm_solve(QbDiisWork& w, int m, int convex, const double* Bin, int ldb,
+                                                const double* v, double* c) {
+    const int M = m + 1;
+    double *B = w.cmB, *A = w.cmA, *W = w.cmW, *b = w.cmb, *x = w.cmx;
+    for (int j = 0; j < m; ++j)
+        for (int i = 0; i < m; ++i) B[i + m * j] = Bin[i + ldb * j];
+    for (int round = 0; round < 64; ++round) {
+        for (int guard = 0; guard < 64; ++guard) {
+            for (int j = 0; j < M; ++j)
+                for (int i = 0; i < M; ++i)
+                    A[i + M * j] = (i < m && j < m) ? B[i + m * j] : ((i == m && j == m) ? 0.0 : 1.0);
+            for (int i = 0; i < M * M; ++i) W[i] = A[i];
+            for (int i = 0; i < M; ++i) x[i] = 0.0;
+            if (qbds::lu_solve(M, W, x) != 0.0) break;
+            for (int i = 0; i < m; ++i) B[i + m * i] += 4e-13;
+        }
+        for (int i = 0; i < m; ++i) b[i] = v ? -v[i] : 0.0;
+        b[m] = 1.0;
+        for (int i = 0; i < M * M; ++i) W[i] = A[i];
+        for (int i = 0; i < M; ++i) x[i] = b[i];
+        qbds::lu_solve(M, W, x);
+        bool neg = false;
+        for (int i = 0; i < m; ++i) {
+            c[i] = x[i];
+            neg |= x[i] < 0.0;
+        }
+        if (!convex || !neg) return true;
+        int perm[QB_DS_N];
+        for (int i = 0; i < m; ++i) perm[i] = i;
+        for (int i = 1; i < m; ++i) {   // stable insertion sort by |c|
+            const int t = perm[i];
+            int j = i - 1;
+            while (j >= 0 && fabs(c[perm[j]]) > fabs(c[t])) {
+                perm[j + 1] = perm[j];
+                --j;
+            }
+            perm[j + 1] = t;
+        }
+        for (int sz = 1; sz <= m; ++sz) {
+            int comb[QB_DS_N];
+            for (int t = 0; t < sz; ++t) comb[t] = t;
+            while (true) {
+                unsigned drop = 0;
+                for (int t = 0; t < sz; ++t) drop |= 1u << perm[comb[t]];
+                int keep[QB_DS_N + 1], k = 0;
+                for (int i = 0; i <= m; ++i)
+                    if (!(drop >> i & 1u)) keep[k++] = i;
+                for (int jj = 0; jj < k; ++jj) {
+                    x[jj] = b[keep[jj]];
+                    for (int ii = 0; ii < k; ++ii) W[ii + k * jj] = A[keep[ii] + M * keep[jj]];
+                }
+                if (qbds::lu_solve(k, W, x) != 0.0) {
+                    bool bad = false;
+                    for (int i = 0; i < m; ++i) c[i] = 0.0;
+                    for (int jj = 0; jj < k - 1; ++jj) c[keep[jj]] = x[jj];
+                    for (int i = 0; i < m; ++i) bad |= c[i] < 0.0;
+                    if (!bad) return true;
+                }
+                int pos = sz - 1;
+                while (pos >= 0 && comb[pos] == m - sz + pos) --pos;
+                if (pos < 0) break;
+                ++comb[pos];
+                for (int t = pos + 1; t < sz; ++t) comb[t] = comb[t - 1] + 1;
+            }
+        }
+        for (int i = 0; i < m; ++i) B[i + m * i] += 4e-13;
+    }
+    return false;
+}
 
 // One thread: solve the DIIS coefficient problem of m entries.  B (m x m, leading
 // dimension ldb) and v (m) describe it; c (m) is the starting point on entry and the
