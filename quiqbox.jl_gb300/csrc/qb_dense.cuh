@@ -215,6 +215,8 @@ __device__ int qb_cta_jacobi(int n, double* A, double* V, const double* Vin, dou
 template <int MAXN>
 struct QbEigSmem {
     double d[MAXN], e[MAXN], lam[MAXN], dots[MAXN];
+    double lamr[MAXN];           // eigenvalue estimates after the FP64 refinement
+    float lamw[MAXN];            // half width of each eigenvalue's FP32 bracket
     float df[MAXN], e2f[MAXN];   // d and e^2 in FP32 for the Sturm counts
     double red[33];
     double bounds[3];
@@ -297,6 +299,19 @@ __device__ __forceinline__ int qb_sturm_f(int n, const float* df, const float* e
         q = (df[j] - x) - __fdividef(e2f[j - 1], q);
         if (fabsf(q) <= tiny) q = -tiny;
         c += q < 0.f;
+    }
+    return c;
+}
+
+// the same count in FP64 (for eigenvalues the FP32 brackets cannot separate)
+__device__ __forceinline__ int qb_sturm_d(int n, const double* d, const double* e, double x, double tiny) {
+    double q = d[0] - x;
+    if (fabs(q) <= tiny) q = -tiny;
+    int c = q < 0.0;
+    for (int j = 1; j < n; ++j) {
+        q = (d[j] - x) - e[j - 1] * e[j - 1] / q;
+        if (fabs(q) <= tiny) q = -tiny;
+        c += q < 0.0;
     }
     return c;
 }
@@ -402,10 +417,11 @@ __device__ void qb_cta_lowest_eig(int n, int k, double* A, double* Y, double* w,
     const float tiny = (float)(1e-30 * nrm) + 1e-30f;
     const float absres = (float)(1e-13 * nrm);
     double* Yt = B0;   // interleaved vectors; B1, B2 and Y hold the interleaved LU factors
-    for (int i0 = 0; i0 < k; i0 += ngrp) {
+    const int kb = k < n ? k + 1 : k;   // one eigenvalue beyond the occupied ones: the gap above them
+    for (int i0 = 0; i0 < kb; i0 += ngrp) {
         const int i = i0 + tid / G;
         float lo = (float)sm.bounds[0], hi = (float)sm.bounds[1];
-        bool frozen = i >= k;
+        bool frozen = i >= kb;
         for (int round = 0; round < 64; ++round) {
             if (__all_sync(0xffffffffu, frozen)) break;
             const float step = (hi - lo) / (float)(G + 1);
@@ -421,8 +437,36 @@ __device__ void qb_cta_lowest_eig(int n, int k, double* A, double* Y, double* w,
                 frozen = !(hi - lo > 2.4e-7f * fmaxf(fabsf(lo), fabsf(hi)) + absres);
             }
         }
-        if (i < k && sub == 0) sm.lam[i] = 0.5 * ((double)lo + (double)hi);
+        if (i < kb && sub == 0) {
+            sm.lam[i] = 0.5 * ((double)lo + (double)hi);
+            sm.lamw[i] = 0.5f * (hi - lo) + absres;
+        }
     }
+    __syncthreads();
+    // an occupied eigenvalue whose FP32 bracket nearly touches a neighbour's (a gap below the
+    // FP32 resolution, e.g. across the occupied/virtual boundary) is bisected again in FP64,
+    // so that inverse iteration separates it from the neighbour
+    for (int i = tid; i < k; i += nt) {
+        const double wi = 4.0 * (double)sm.lamw[i];
+        const bool near = (i > 0 && sm.lam[i] - sm.lam[i - 1] <= wi + 4.0 * (double)sm.lamw[i - 1]) ||
+                          (i + 1 < kb && sm.lam[i + 1] - sm.lam[i] <= wi + 4.0 * (double)sm.lamw[i + 1]);
+        sm.lamr[i] = sm.lam[i];
+        if (!near) continue;
+        const double tinyd = 1e-300 + 1e-290 * nrm;
+        double lo = sm.lam[i] - 2.0 * wi, hi = sm.lam[i] + 2.0 * wi;
+        if (!(qb_sturm_d(n, sm.d, sm.e, lo, tinyd) <= i && qb_sturm_d(n, sm.d, sm.e, hi, tinyd) > i)) {
+            lo = sm.bounds[0];   // the FP32 bracket missed the eigenvalue: start from Gershgorin
+            hi = sm.bounds[1];
+        }
+        for (int it = 0; it < 120 && hi - lo > 4.0 * 2.220446049250313e-16 * nrm; ++it) {
+            const double mid = 0.5 * (lo + hi);
+            if (qb_sturm_d(n, sm.d, sm.e, mid, tinyd) > i) hi = mid;
+            else lo = mid;
+        }
+        sm.lamr[i] = 0.5 * (lo + hi);
+    }
+    __syncthreads();
+    for (int i = tid; i < k; i += nt) sm.lam[i] = sm.lamr[i];
     __syncthreads();
     // inverse iteration at the fixed FP32 shift (within ~1e-7 ||T|| of the eigenvalue):
     // components of eigenvalues further than 1e-4 ||T|| shrink by >= 1e3 per step, so four

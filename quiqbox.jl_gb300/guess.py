@@ -453,7 +453,13 @@ def evaluate(qb, net, n_test=2000, seed=202, fallback_iter=FALLBACK_ITER):
     t_guess = time.perf_counter() - t0
     both = base.converged & lrn.converged
     dE = np.abs(base.energies[both] - lrn.energies[both])
+    signed = lrn.energies - base.energies
+    same = both & (np.abs(signed) < 1e-8)
     return {"molecules": n_test, "coreh_converged": int(base.converged.sum()),
+            "learned_same_state": int(same.sum()),
+            "learned_lower_state": int((both & (signed <= -1e-8)).sum()),
+            "learned_higher_state": int((both & (signed >= 1e-8)).sum()),
+            "learned_same_state_solves_per_s": float(same.sum() / t_lrn),
             "learned_converged": int(lrn.converged.sum()), "fallback_iter": fallback_iter,
             "restarted_from_coreh": len(redo),
             "coreh_mean_iterations": float(base.iterations[both].mean()),

@@ -64,3 +64,24 @@ def test_degenerate_and_h2_like(qb):
     w[1::2] += 1e-7
     _check(qb, Q @ np.diag(w) @ Q.T, 12, tol=1e-9)
     _check(qb, 1e4 * np.eye(30) + (lambda M: M + M.T)(rng.normal(size=(30, 30))), 12, tol=1e-10)
+
+
+def test_gap_inside_fp32_bracket(qb):
+    # The gap between the highest occupied (k-1) and the lowest unoccupied (k) eigenvalue
+    # below the FP32 bisection's resolution (~2.4e-7 ||T||): the eigensolver refines those
+    # eigenvalues in FP64 and the occupied density still matches numpy's FP64 eigh, to the
+    # accuracy such a gap allows any FP64 solver (~eps ||A|| / gap).
+    rng = np.random.default_rng(21)
+    for n, k, gap in ((20, 7, 1e-8), (48, 20, 3e-8), (64, 31, 1e-9), (116, 40, 5e-8)):
+        Q = np.linalg.qr(rng.normal(size=(n, n)))[0]
+        w = np.sort(rng.uniform(-2.0, 2.0, size=n))
+        w[k] = w[k - 1] + gap
+        A = Q @ np.diag(w) @ Q.T
+        A = 0.5 * (A + A.T)
+        wq, Y = qb.api.eigh_lowest(A, k)
+        wr, Vr = np.linalg.eigh(A)
+        scale = np.abs(wr).max()
+        assert wr[k] - wr[k - 1] < 2.4e-7 * scale
+        assert np.abs(wq - wr[:k]).max() < 1e-10 * scale
+        D, Dr = Y @ Y.T, Vr[:, :k] @ Vr[:, :k].T
+        assert np.abs(D - Dr).max() < max(100 * 2.220446049250313e-16 * scale / gap, 1e-10), (n, k, gap)
