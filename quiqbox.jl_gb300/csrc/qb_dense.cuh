@@ -443,15 +443,30 @@ __device__ void qb_cta_lowest_eig(int n, int k, double* A, double* Y, double* w,
         }
     }
     __syncthreads();
-    // an occupied eigenvalue whose FP32 bracket nearly touches a neighbour's (a gap below the
-    // FP32 resolution, e.g. across the occupied/virtual boundary) is bisected again in FP64,
-    // so that inverse iteration separates it from the neighbour
+    // a gap between the highest occupied eigenvalue and the next one below the FP32
+    // resolution: the occupied eigenvalues of that boundary cluster (each within its FP32
+    // bracket of the next) are bisected again in FP64, so that inverse iteration separates
+    // the occupied vectors from the unoccupied neighbour.  Clusters inside the occupied
+    // set need no such care (Gram-Schmidt below orthogonalises them).
+    __shared__ int s_lo;
+    if (tid == 0) {
+        s_lo = k;
+        if (kb > k) {
+            int j = k - 1;
+            auto near = [&](int a) {   // eigenvalues a and a + 1 within their FP32 brackets
+                return sm.lam[a + 1] - sm.lam[a] <= 4.0 * ((double)sm.lamw[a] + (double)sm.lamw[a + 1]);
+            };
+            while (j >= 0 && near(j)) {
+                s_lo = j;
+                --j;
+            }
+        }
+    }
+    __syncthreads();
     for (int i = tid; i < k; i += nt) {
-        const double wi = 4.0 * (double)sm.lamw[i];
-        const bool near = (i > 0 && sm.lam[i] - sm.lam[i - 1] <= wi + 4.0 * (double)sm.lamw[i - 1]) ||
-                          (i + 1 < kb && sm.lam[i + 1] - sm.lam[i] <= wi + 4.0 * (double)sm.lamw[i + 1]);
         sm.lamr[i] = sm.lam[i];
-        if (!near) continue;
+        if (i < s_lo) continue;
+        const double wi = 4.0 * (double)sm.lamw[i];
         const double tinyd = 1e-300 + 1e-290 * nrm;
         double lo = sm.lam[i] - 2.0 * wi, hi = sm.lam[i] + 2.0 * wi;
         if (!(qb_sturm_d(n, sm.d, sm.e, lo, tinyd) <= i && qb_sturm_d(n, sm.d, sm.e, hi, tinyd) > i)) {
