@@ -88,7 +88,6 @@ struct MolDev {
     double *Gee, *Gdf;              // pool x pool: <e'_a, e'_b>, <D_a, F_b>
     double *eps, *wt;
     const double* ratio;
-    QbDiisWork* dw;
 };
 
 struct StepParams {
@@ -416,6 +415,8 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
     __shared__ double s_B[QB_BATCH_DIIS * QB_BATCH_DIIS], s_v[QB_BATCH_DIIS];
     __shared__ int s_idx[QB_BATCH_POOL], s_slot, s_nlive, s_act, s_stale, s_needF;
     __shared__ double s_diis[QB_BATCH_DIIS + 2][QB_BATCH_DIIS + 3];
+    extern __shared__ __align__(16) unsigned char s_dyn[];   // the coefficient solver's state
+    QbDiisWork& sw = *reinterpret_cast<QbDiisWork*>(s_dyn);
     MolDev& M = mols[order[blockIdx.x]];
     if (M.conv) return;
     const int n = M.n, nn = n * n, tid = threadIdx.x, nt = blockDim.x;
@@ -734,8 +735,8 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
                 }
             }
         } else if (tid == 0) {
-            if (sv == QB_DIIS_LCM) qb_cm_solve(*M.dw, m, meth != QB_SCF_DIIS, s_B, m, s_v, M.c);
-            else qb_diis_iterative_solve(*M.dw, sv, meth != QB_SCF_DIIS, m, s_B, m, s_v, M.c);
+            if (sv == QB_DIIS_LCM) qb_cm_solve(sw, m, meth != QB_SCF_DIIS, s_B, m, s_v, M.c);
+            else qb_diis_iterative_solve(sw, sv, meth != QB_SCF_DIIS, m, s_B, m, s_v, M.c);
         }
         __syncthreads();
         // F = sum_k c_k F_k (AO) -> F' = X^T F X
@@ -939,11 +940,9 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     const int nbase = 17;   // S, H, X, S^1/2, F, D, Dt, D', J', K', C', 6 work matrices
     const int nmat = nbase + 3 * QB_BATCH_POOL;
     DevArray<double> d_mats, d_vecs, d_G;
-    DevArray<QbDiisWork> d_dw;
     QB_CUDA(ctx, d_mats.ensure((size_t)nmat * NN));
     QB_CUDA(ctx, d_vecs.ensure(2 * (size_t)vo[nmol]));
     QB_CUDA(ctx, d_G.ensure((size_t)nmol * 2 * QB_BATCH_POOL * QB_BATCH_POOL));
-    QB_CUDA(ctx, d_dw.ensure(nmol));
     QB_CUDA(ctx, cudaMemsetAsync(d_G.p, 0, (size_t)nmol * 2 * QB_BATCH_POOL * QB_BATCH_POOL * sizeof(double), s));
     std::vector<MolDev> hm(nmol);
     for (int m = 0; m < nmol; ++m) {
@@ -961,7 +960,7 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
         M.Es = d_mats.p + (size_t)(nbase + 2 * QB_BATCH_POOL) * NN + (size_t)QB_BATCH_POOL * mo[m];
         M.Gee = d_G.p + (size_t)m * 2 * QB_BATCH_POOL * QB_BATCH_POOL;
         M.Gdf = M.Gee + QB_BATCH_POOL * QB_BATCH_POOL;
-        M.dw = d_dw.p + m;
+
         M.eps = d_vecs.p + vo[m];
         M.wt = d_vecs.p + vo[nmol] + vo[m];
         M.ratio = d_ratio.p + fo[m];
@@ -1244,8 +1243,10 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
             if (nch == 0) continue;
             kClasses[c].digest(work[c], d_chunks.p + chunk_at[c], d_eri.p + eri_at[c], d_mols.p, nch, st);
         }
-        qb_batch_step_kernel<<<nmol, QB_BATCH_THREADS, 0, st>>>(d_mols.p, d_order.p, prm, d_active);
+        qb_batch_step_kernel<<<nmol, QB_BATCH_THREADS, sizeof(QbDiisWork), st>>>(d_mols.p, d_order.p, prm, d_active);
     };
+    QB_CUDA(ctx, cudaFuncSetAttribute(qb_batch_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(QbDiisWork)));
     // every molecule needs at most 2 passes per SCF step, plus the guesses (a restart doubles them)
     const int cap = 2 * cfg.max_iter + 8;
     int launches = 0;

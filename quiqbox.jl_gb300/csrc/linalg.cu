@@ -225,24 +225,28 @@ void qb_lincomb(cudaStream_t s, long long len, int m, const double* const* mats,
 // ---------------------------------------------------------------------------
 // DIIS coefficient problem: the Lagrange-multiplier solver (qb_cm_solve, CMsolver!,
 // HartreeFock.jl:1445-1477) or the iterative ones (qb_diis_iterative_solve), one thread,
-// state in the caller's QbDiisWork.
+// its state in shared memory (a single thread's read-after-write traffic through global
+// memory would go to L2 at every step).
 #define QB_DIIS_MAX 16
-__global__ void qb_diis_cm_kernel(int m, int convex, const double* B, const double* v, double* c, QbDiisWork* work,
-                                  int* status) {
-    if (threadIdx.x == 0 && blockIdx.x == 0 && !qb_cm_solve(*work, m, convex, B, m, v, c)) atomicOr(status, 4);
+__global__ void qb_diis_cm_kernel(int m, int convex, const double* B, const double* v, double* c, int* status) {
+    __shared__ QbDiisWork sw;
+    if (threadIdx.x == 0 && blockIdx.x == 0 && !qb_cm_solve(sw, m, convex, B, m, v, c)) atomicOr(status, 4);
 }
 
 // L-BFGS-B / SPG solve by one thread (qb_diis_solvers.cuh); c holds the starting point.
 __global__ void qb_diis_iter_kernel(int solver, int convex, int m, const double* B, const double* v, double* c,
-                                    QbDiisWork* work) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) qb_diis_iterative_solve(*work, solver, convex, m, B, m, v, c);
+                                    int* iters) {
+    __shared__ QbDiisWork sw;
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const int it = qb_diis_iterative_solve(sw, solver, convex, m, B, m, v, c);
+        if (iters) *iters = it;
+    }
 }
 
 int qb_diis_solve(cudaStream_t s, int m, int convex, int solver, const double* B, const double* v, double* c,
-                  QbDiisWork* work, int* status) {
-    if (m < 1 || m > QB_DIIS_MAX) return -1;
-    if (!work || m > QB_DS_N) return -1;
-    if (solver == QB_DIIS_LCM) qb_diis_cm_kernel<<<1, 32, 0, s>>>(m, convex, B, v, c, work, status);
-    else qb_diis_iter_kernel<<<1, 32, 0, s>>>(solver, convex, m, B, v, c, work);
+                  int* iters, int* status) {
+    if (m < 1 || m > QB_DIIS_MAX || m > QB_DS_N) return -1;
+    if (solver == QB_DIIS_LCM) qb_diis_cm_kernel<<<1, 32, 0, s>>>(m, convex, B, v, c, status);
+    else qb_diis_iter_kernel<<<1, 32, 0, s>>>(solver, convex, m, B, v, c, iters);
     return 0;
 }

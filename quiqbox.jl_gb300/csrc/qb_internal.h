@@ -176,7 +176,6 @@ void qb_jk_finalize(cudaStream_t s, int n, const double* ratio, const double* Jp
                     double* K);
 void qb_density_prescale(cudaStream_t s, int n, const double* ratio, const double* D, double* Dt, double* dmax);
 void qb_gwh(cudaStream_t s, int n, const double* S, const double* H, double* out);
-struct QbDiisWork;
 int qb_diis_solve(cudaStream_t s, int m, int convex, int solver, const double* B, const double* v, double* c,
-                  QbDiisWork* work, int* status);
+                  int* iters, int* status);
 void qb_lincomb(cudaStream_t s, long long len, int m, const double* const* mats, const double* c, double* out);

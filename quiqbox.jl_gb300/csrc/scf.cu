@@ -149,7 +149,6 @@ struct Scf {
            *E_d = nullptr;
     const double** ptrs_d = nullptr;
     const double** ptrs2_d = nullptr;
-    QbDiisWork* dwork = nullptr;   // state of the iterative DIIS coefficient solvers
     std::vector<std::unique_ptr<double, void (*)(void*)>> owned;
 
     double* alloc(size_t count) {
@@ -177,11 +176,6 @@ struct Scf {
         owned.emplace_back((double*)p2, [](void* q) { cudaFree(q); });
         ptrs_d = (const double**)p1;
         ptrs2_d = (const double**)p2;
-        void* p3 = nullptr;
-        if (cudaMalloc(&p3, sizeof(QbDiisWork)) != cudaSuccess)
-            return qb_set_error(ctx, QB_ERR_NOMEM, "DIIS solver workspace");
-        owned.emplace_back((double*)p3, [](void* q) { cudaFree(q); });
-        dwork = (QbDiisWork*)p3;
         if (!S || !H || !X || !t1 || !t2 || !t3 || !J || !K || !eigw || !eigwork || !scal || !gram || !B || !v ||
             !c || !E_d)
             return qb_set_error(ctx, QB_ERR_NOMEM, "SCF device buffers");
@@ -447,7 +441,7 @@ int run_core(Scf& sc, Core& core, RunState& st, StepOut& out) {
         QB_CUDA(sc.ctx, cudaMemcpyAsync(sc.c, core.cs[k].data(), m * sizeof(double), cudaMemcpyHostToDevice, sc.s));
         gram_kernel<<<dim3(m, m), 256, 0, sc.s>>>(m, (long long)sc.nn, sc.ptrs_d, sc.ptrs2_d, sc.gram);
         diis_system_kernel<<<1, dim3(16, 16), 0, sc.s>>>(m, core.method, sc.gram, sc.E_d, sc.B, sc.v);
-        if (qb_diis_solve(sc.s, m, core.method != QB_SCF_DIIS, core.solver, sc.B, sc.v, sc.c, sc.dwork,
+        if (qb_diis_solve(sc.s, m, core.method != QB_SCF_DIIS, core.solver, sc.B, sc.v, sc.c, nullptr,
                           sc.ctx->status.p) != 0)
             return qb_set_error(sc.ctx, QB_ERR_ARG, "DIIS subspace size or solver out of range");
         std::vector<const double*> Fp(m);
@@ -653,30 +647,25 @@ extern "C" int qb_diis_coefficients(qb_ctx* ctx, int solver, int convex, int m, 
     if (solver < QB_DIIS_LBFGS || solver > QB_DIIS_LCM) return qb_set_error(ctx, QB_ERR_ARG, "unknown solver");
     if (cudaSetDevice(ctx->device) != cudaSuccess) return qb_set_error(ctx, QB_ERR_CUDA, "cudaSetDevice");
     cudaStream_t s = ctx->stream;
-    const size_t bytes = (size_t)m * m * sizeof(double) + 2 * (size_t)m * sizeof(double);
+    const size_t bytes = (size_t)m * m * sizeof(double) + 2 * (size_t)m * sizeof(double) + sizeof(double);
     double* buf = nullptr;
-    QbDiisWork* w = nullptr;
     if (cudaMalloc(&buf, bytes) != cudaSuccess) return qb_set_error(ctx, QB_ERR_NOMEM, "DIIS buffers");
-    if (cudaMalloc(&w, sizeof(QbDiisWork)) != cudaSuccess) {
-        cudaFree(buf);
-        return qb_set_error(ctx, QB_ERR_NOMEM, "DIIS solver workspace");
-    }
     double *dB = buf, *dv = buf + (size_t)m * m, *dc = dv + m;
+    int* dit = reinterpret_cast<int*>(dc + m);
     std::vector<double> vz(m, 0.0);
     int rc = QB_OK;
     rc = qb_cuda_check(ctx, cudaMemcpyAsync(dB, B, (size_t)m * m * sizeof(double), cudaMemcpyHostToDevice, s), "B");
     if (rc == QB_OK)
         rc = qb_cuda_check(ctx, cudaMemcpyAsync(dv, v ? v : vz.data(), m * sizeof(double), cudaMemcpyHostToDevice, s), "v");
     if (rc == QB_OK) rc = qb_cuda_check(ctx, cudaMemcpyAsync(dc, c, m * sizeof(double), cudaMemcpyHostToDevice, s), "c");
-    if (rc == QB_OK && qb_diis_solve(s, m, convex != 0, solver, dB, dv, dc, w, ctx->status.p) != 0)
+    if (rc == QB_OK) rc = qb_cuda_check(ctx, cudaMemsetAsync(dit, 0, sizeof(int), s), "iterations");
+    if (rc == QB_OK && qb_diis_solve(s, m, convex != 0, solver, dB, dv, dc, dit, ctx->status.p) != 0)
         rc = qb_set_error(ctx, QB_ERR_ARG, "DIIS solve");
     if (rc == QB_OK) rc = qb_cuda_check(ctx, cudaMemcpyAsync(c, dc, m * sizeof(double), cudaMemcpyDeviceToHost, s), "c");
     int it = 0;
-    if (rc == QB_OK && iterations)
-        rc = qb_cuda_check(ctx, cudaMemcpyAsync(&it, &w->iters, sizeof(int), cudaMemcpyDeviceToHost, s), "iters");
+    if (rc == QB_OK) rc = qb_cuda_check(ctx, cudaMemcpyAsync(&it, dit, sizeof(int), cudaMemcpyDeviceToHost, s), "iters");
     if (rc == QB_OK) rc = qb_cuda_check(ctx, cudaStreamSynchronize(s), "DIIS solve");
     cudaFree(buf);
-    cudaFree(w);
     if (rc != QB_OK) return rc;
     if (iterations) *iterations = solver == QB_DIIS_LCM ? 0 : it;
     return qb_check_status(ctx);
