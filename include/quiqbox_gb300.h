@@ -296,6 +296,8 @@ typedef struct {
     int graph_launches;     /* 1: the whole iteration ran as one graph launch */
     double* density;        /* NULL or room for the final per-spin densities, concatenated */
     int* restarted;         /* NULL or nmol: 1 if the molecule restarted from the core-Hamiltonian guess */
+    int digest_chunk;       /* quartets per digest block chosen by timing on this batch (molecules with
+                               little work in a class use a quarter of it) */
 } qb_batch_result;
 
 void qb_batch_config_default(qb_batch_config* cfg);

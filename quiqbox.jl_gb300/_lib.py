@@ -181,7 +181,7 @@ class QBBatchResult(C.Structure):
                 ("converged", C.POINTER(C.c_int)), ("jacobi_sweeps", C.POINTER(C.c_int)),
                 ("ms_integrals", C.c_double), ("ms_scf", C.c_double), ("quartets", C.c_int64),
                 ("prim_quartets", C.c_int64), ("eri_doubles", C.c_int64), ("graph_launches", C.c_int),
-                ("density", C.POINTER(C.c_double)), ("restarted", C.POINTER(C.c_int))]
+                ("density", C.POINTER(C.c_double)), ("restarted", C.POINTER(C.c_int)), ("digest_chunk", C.c_int)]
 
 
 class BasisArgs:

@@ -420,6 +420,7 @@ class BatchSCFResult:
     graph_launches: int
     densities: Optional[list] = None   # final per-spin densities (return_densities=True)
     restarted: Optional[np.ndarray] = None   # restarted from the core-Hamiltonian guess (fallback_iter)
+    digest_chunk: int = 0                    # digest chunk size chosen by timing on the batch
 
 
 _TRIU = {}
@@ -537,7 +538,7 @@ def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ct
             off += n * n
     return BatchSCFResult(E + enn, E, it, conv.astype(bool), sw, np.array(nf), res.ms_integrals,
                           res.ms_scf, int(res.quartets), int(res.prim_quartets), int(res.eri_doubles),
-                          int(res.graph_launches), dens, rst.astype(bool))
+                          int(res.graph_launches), dens, rst.astype(bool), int(res.digest_chunk))
 
 
 def fp64_peak(ctx=None):

@@ -1154,32 +1154,69 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
         cd.store(work[c], d_prims.p, ctx->boys.p, d_eri.p + eri_at[c], d_primcount.p, d_perm.p, grid, s);
     }
     QB_CUDA(ctx, cudaGetLastError());
-    // ---- digest chunks: per class and molecule, runs of at most QB_DIGEST_CHUNK quartets
-    // (QB_DIGEST_CHUNK_SMALL for a molecule with fewer than 128 such runs in the class: its
-    // late iterations then still spread over many SMs)
+    // ---- digest chunks: per class and molecule, runs of at most `big` quartets (`small` for
+    // a molecule with fewer than 128 such runs in the class: its late iterations then still
+    // spread over many SMs).  The sizes are tuned on this batch: one digest pass of every
+    // class timed per candidate pair before the iterations start (the densities are zeroed
+    // for it, and J', K' after it).
     std::vector<DigestChunk> h_chunks;
     std::vector<size_t> chunk_at(QB_BATCH_NCLASS + 1, 0);
-    for (int c = 0; c < QB_BATCH_NCLASS; ++c) {
-        chunk_at[c] = h_chunks.size();
-        const ClassDef& cd = kClasses[c];
-        const int X = pc_of(cd.la, cd.lb);
-        const long long* off = h_offs.data() + offs_at[c];
-        for (int m = 0; m < nmol; ++m) {
-            const int s0 = seg[X][m], s1 = seg[X][m + 1];
-            const long long chunk = (off[s1] - off[s0]) >= 128LL * QB_DIGEST_CHUNK ? QB_DIGEST_CHUNK
-                                                                                   : QB_DIGEST_CHUNK_SMALL;
-            for (long long t0 = off[s0]; t0 < off[s1]; t0 += chunk) {
-                const long long t1 = std::min<long long>(t0 + chunk, off[s1]);
-                // bras owning [t0, t1): largest b with off[b] <= t0, one past the largest with off[b] <= t1 - 1
-                const int b0 = (int)(std::upper_bound(off + s0, off + s1, t0) - off) - 1;
-                const int b1 = (int)(std::upper_bound(off + s0, off + s1, t1 - 1) - off);
-                h_chunks.push_back(DigestChunk{t0, t1, b0, b1, m, 0});
+    auto build_chunks = [&](long long big, long long small) {
+        h_chunks.clear();
+        for (int c = 0; c < QB_BATCH_NCLASS; ++c) {
+            chunk_at[c] = h_chunks.size();
+            const ClassDef& cd = kClasses[c];
+            const int X = pc_of(cd.la, cd.lb);
+            const long long* off = h_offs.data() + offs_at[c];
+            for (int m = 0; m < nmol; ++m) {
+                const int s0 = seg[X][m], s1 = seg[X][m + 1];
+                const long long chunk = (off[s1] - off[s0]) >= 128LL * big ? big : small;
+                for (long long t0 = off[s0]; t0 < off[s1]; t0 += chunk) {
+                    const long long t1 = std::min<long long>(t0 + chunk, off[s1]);
+                    // bras owning [t0, t1): largest b with off[b] <= t0, one past the largest with off[b] <= t1 - 1
+                    const int b0 = (int)(std::upper_bound(off + s0, off + s1, t0) - off) - 1;
+                    const int b1 = (int)(std::upper_bound(off + s0, off + s1, t1 - 1) - off);
+                    h_chunks.push_back(DigestChunk{t0, t1, b0, b1, m, 0});
+                }
             }
         }
-    }
-    chunk_at[QB_BATCH_NCLASS] = h_chunks.size();
+        chunk_at[QB_BATCH_NCLASS] = h_chunks.size();
+    };
+    static const long long kChunkCand[3][2] = {{QB_DIGEST_CHUNK / 2, QB_DIGEST_CHUNK_SMALL / 2},
+                                               {QB_DIGEST_CHUNK, QB_DIGEST_CHUNK_SMALL},
+                                               {2 * QB_DIGEST_CHUNK, 2 * QB_DIGEST_CHUNK_SMALL}};
+    build_chunks(kChunkCand[0][0], kChunkCand[0][1]);   // the finest split has the most chunks
     DevArray<DigestChunk> d_chunks;
     QB_CUDA(ctx, d_chunks.ensure(std::max<size_t>(1, h_chunks.size())));
+    int best_cand = 1;
+    {
+        QB_CUDA(ctx, cudaMemsetAsync(d_mats.p + 5 * (size_t)NN, 0, NN * sizeof(double), s));   // D~
+        float best_ms = -1.f;
+        for (int k = 0; k < 3; ++k) {
+            build_chunks(kChunkCand[k][0], kChunkCand[k][1]);
+            if (h_chunks.empty()) break;
+            QB_CUDA(ctx, cudaMemcpyAsync(d_chunks.p, h_chunks.data(), h_chunks.size() * sizeof(DigestChunk),
+                                         cudaMemcpyHostToDevice, s));
+            float ms = 0.f;
+            for (int rep = 0; rep < 2; ++rep) {   // the first pass warms the caches
+                QB_CUDA(ctx, cudaEventRecord(ctx->ev_start, s));
+                for (int c = 0; c < QB_BATCH_NCLASS; ++c) {
+                    const int nch = (int)(chunk_at[c + 1] - chunk_at[c]);
+                    if (nch > 0)
+                        kClasses[c].digest(work[c], d_chunks.p + chunk_at[c], d_eri.p + eri_at[c], d_mols.p, nch, s);
+                }
+                QB_CUDA(ctx, cudaEventRecord(ctx->ev_stop, s));
+                QB_CUDA(ctx, cudaEventSynchronize(ctx->ev_stop));
+                QB_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+            }
+            if (best_ms < 0.f || ms < best_ms) {
+                best_ms = ms;
+                best_cand = k;
+            }
+        }
+        QB_CUDA(ctx, cudaMemsetAsync(d_mats.p + 7 * (size_t)NN, 0, 2 * NN * sizeof(double), s));   // J', K'
+    }
+    build_chunks(kChunkCand[best_cand][0], kChunkCand[best_cand][1]);
     if (!h_chunks.empty())
         QB_CUDA(ctx, cudaMemcpyAsync(d_chunks.p, h_chunks.data(), h_chunks.size() * sizeof(DigestChunk),
                                      cudaMemcpyHostToDevice, s));
@@ -1335,6 +1372,7 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     res->prim_quartets = (int64_t)nprimq;
     res->eri_doubles = (int64_t)eri_at[QB_BATCH_NCLASS];
     res->graph_launches = launches;
+    res->digest_chunk = (int)kChunkCand[best_cand][0];
     int failed = 0;
     for (int m = 0; m < nmol; ++m) {
         if (res->energy) res->energy[m] = hm[m].E;

@@ -23,6 +23,7 @@ def test_batched_rhf_vs_oracle(qb, oracle):
     res = qb.runHartreeFockBatched([(m["nuc"], m["flat"], m["charge"]) for m in mols])
     assert res.converged.all(), res.iterations
     assert res.graph_launches == 1   # every iteration of every molecule in one graph launch
+    assert res.digest_chunk in (1024, 2048, 4096)   # chosen by timing on this batch
     steps = []
     for k, m in enumerate(mols):
         ro = _oracle_rhf(oracle, m)
