@@ -734,7 +734,7 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
                     M.c[m - 1] = 1.0;
                 }
             }
-        } else if (tid == 0) {
+        } else if (tid < 32) {
             if (sv == QB_DIIS_LCM) qb_cm_solve(sw, m, meth != QB_SCF_DIIS, s_B, m, s_v, M.c);
             else qb_diis_iterative_solve(sw, sv, meth != QB_SCF_DIIS, m, s_B, m, s_v, M.c);
         }

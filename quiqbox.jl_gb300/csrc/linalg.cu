@@ -224,22 +224,24 @@ void qb_lincomb(cudaStream_t s, long long len, int m, const double* const* mats,
 
 // ---------------------------------------------------------------------------
 // DIIS coefficient problem: the Lagrange-multiplier solver (qb_cm_solve, CMsolver!,
-// HartreeFock.jl:1445-1477) or the iterative ones (qb_diis_iterative_solve), one thread,
-// its state in shared memory (a single thread's read-after-write traffic through global
-// memory would go to L2 at every step).
+// HartreeFock.jl:1445-1477) or the iterative ones (qb_diis_iterative_solve), one warp,
+// its state in shared memory.
 #define QB_DIIS_MAX 16
 __global__ void qb_diis_cm_kernel(int m, int convex, const double* B, const double* v, double* c, int* status) {
     __shared__ QbDiisWork sw;
-    if (threadIdx.x == 0 && blockIdx.x == 0 && !qb_cm_solve(sw, m, convex, B, m, v, c)) atomicOr(status, 4);
+    if (threadIdx.x < 32 && blockIdx.x == 0) {
+        const bool ok = qb_cm_solve(sw, m, convex, B, m, v, c);
+        if (!ok && threadIdx.x == 0) atomicOr(status, 4);
+    }
 }
 
-// L-BFGS-B / SPG solve by one thread (qb_diis_solvers.cuh); c holds the starting point.
+// L-BFGS-B / SPG solve by one warp (qb_diis_solvers.cuh); c holds the starting point.
 __global__ void qb_diis_iter_kernel(int solver, int convex, int m, const double* B, const double* v, double* c,
                                     int* iters) {
     __shared__ QbDiisWork sw;
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
+    if (threadIdx.x < 32 && blockIdx.x == 0) {
         const int it = qb_diis_iterative_solve(sw, solver, convex, m, B, m, v, c);
-        if (iters) *iters = it;
+        if (iters && threadIdx.x == 0) *iters = it;
     }
 }
 

@@ -17,12 +17,20 @@
 // Moré & Thuente (ACM TOMS 20, 1994); SPG is SPG2 of Birgin, Martínez & Raydan (SIAM J.
 // Optim. 10, 2000).
 //
-// The problems have at most 16 variables, so one thread runs a solve; its state lives in
-// a QbDiisWork block in global memory supplied by the caller (about 20 KB), never in the
-// thread's local frame.  Every loop is bounded (10000 iterations and evaluations, 20 trial
-// steps per line search, as in the reference's settings).  The starting point is c on
-// entry (the previous solution with a 1 appended for the newest entry, as the reference's
-// per-method coefficient vector carries over); on return c holds the normalised solution.
+// One warp runs a solve.  The problems have at most 16 variables and 15 correction pairs
+// (30 rows in the compact L-BFGS-B matrices), so lane i owns variable i, or row / column i
+// of a small matrix, and the scalar control (line search, breakpoint walk, stopping tests)
+// runs alike in every lane from values that every lane holds.  GB300 issues an FP64 warp
+// instruction in about 64 cycles per SM sub-partition whether one lane or 32 are active, so
+// a one-thread solver pays that for every scalar operation; spreading the vector and matrix
+// loops over the lanes divides the instruction count by up to 32.  Sums over lanes are
+// butterfly reductions, which give the same value in every lane.  The state lives in a
+// QbDiisWork block in shared memory supplied by the caller (about 27 KB).  Every loop is
+// bounded (10000 iterations and evaluations, 20 trial steps per line search, as in the
+// reference's settings).  The starting point is c on entry (the previous solution with a 1
+// appended for the newest entry, as the reference's per-method coefficient vector carries
+// over); on return c holds the normalised solution.  All 32 lanes of the warp must call the
+// entry points together.
 #pragma once
 #include "quiqbox_gb300.h"   // QB_DIIS_LBFGS / QB_DIIS_SPGB / QB_DIIS_LCM
 
@@ -36,40 +44,71 @@ struct QbDiisWork {
     double wn[4 * QB_DS_M * QB_DS_M];
     double x[QB_DS_N], g[QB_DS_N], z[QB_DS_N], d[QB_DS_N], r[QB_DS_N], xs[QB_DS_N], gs[QB_DS_N], xp[QB_DS_N];
     double cw[2 * QB_DS_M], p[2 * QB_DS_M], vv[2 * QB_DS_M], wbp[2 * QB_DS_M], wv[2 * QB_DS_M];
-    double tb[QB_DS_N], fprev[20];
+    double rinv[2 * QB_DS_M];            // reciprocal diagonal of a triangular factor
+    double dinv[QB_DS_M], sqinv[QB_DS_M];  // 1 / SY(k,k) and 1 / sqrt(SY(k,k))
+    double fprev[20];
     double cmB[QB_DS_N * QB_DS_N], cmA[(QB_DS_N + 1) * (QB_DS_N + 1)], cmW[(QB_DS_N + 1) * (QB_DS_N + 1)];
     double cmb[QB_DS_N + 1], cmx[QB_DS_N + 1];
-    int ord[QB_DS_N], where[QB_DS_N], freel[QB_DS_N], actl[QB_DS_N];
-    int nfree, nact;
+    int where[QB_DS_N], freel[QB_DS_N];
     int iters;   // solver iterations of the last solve (diagnostics)
 };
 
 namespace qbds {
 
+constexpr unsigned kFull = 0xffffffffu;
 constexpr double kEps = 2.220446049250313e-16;
 constexpr double kShift = 4e-16;   // getAtolVal(Float64) (src/Arithmetic.jl:42)
 
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+__device__ __forceinline__ double wsum(double a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
+    return a;
+}
+
+__device__ __forceinline__ double wmax(double a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a = fmax(a, __shfl_xor_sync(kFull, a, o));
+    return a;
+}
+
+// Smallest value over the lanes and the lowest lane holding it.
+__device__ __forceinline__ double wargmin(double a, int& at) {
+    double m = a;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(kFull, m, o));
+    at = __ffs(__ballot_sync(kFull, a == m)) - 1;
+    return m;
+}
+
+__device__ __forceinline__ bool wany(bool p) { return __any_sync(kFull, p); }
+
 // shiftLastEle! on the iterate
 __device__ inline double shifted_sum(int n, double* c) {
-    double s = 0.0;
-    for (int i = 0; i < n; ++i) s += c[i];
+    const int l = lane_id();
+    double s = wsum(l < n ? c[l] : 0.0);
     if (s < kShift) {
         const double sh = (s < 0 ? -1.0 : 1.0) * kShift;
         s += sh;
-        c[n - 1] += sh;
+        __syncwarp();
+        if (l == n - 1) c[l] += sh;
+        __syncwarp();
     }
     return s;
 }
 
+// v.c and c^T B c
 __device__ inline void parts(const QbDiisWork& w, int n, const double* c, double& vc, double& cBc) {
-    vc = 0.0;
-    cBc = 0.0;
-    for (int j = 0; j < n; ++j) {
-        vc += w.v[j] * c[j];
-        double t = 0.0;
-        for (int i = 0; i < n; ++i) t += c[i] * w.B[i + QB_DS_N * j];
-        cBc += t * c[j];
+    const int l = lane_id();
+    double t = 0.0, cl = 0.0, vl = 0.0;
+    if (l < n) {
+        cl = c[l];
+        vl = w.v[l];
+        for (int i = 0; i < n; ++i) t = fma(c[i], w.B[i + QB_DS_N * l], t);
     }
+    vc = wsum(vl * cl);
+    cBc = wsum(t * cl);
 }
 
 __device__ inline double obj_f(const QbDiisWork& w, int n, double* c) {
@@ -84,11 +123,13 @@ __device__ inline void obj_g(const QbDiisWork& w, int n, double* c, double* g) {
     double vc, cBc;
     parts(w, n, c, vc, cBc);
     const double common = vc / (s * s) + cBc / (s * s * s);
-    for (int i = 0; i < n; ++i) {
+    const int l = lane_id();
+    if (l < n) {
         double bc = 0.0;
-        for (int j = 0; j < n; ++j) bc += (w.B[i + QB_DS_N * j] + w.B[j + QB_DS_N * i]) * c[j];
-        g[i] = w.v[i] / s + bc / (2 * s * s) - common;
+        for (int j = 0; j < n; ++j) bc = fma(w.B[l + QB_DS_N * j] + w.B[j + QB_DS_N * l], c[j], bc);
+        g[l] = w.v[l] / s + bc / (2 * s * s) - common;
     }
+    __syncwarp();
 }
 
 __device__ inline double fg(const QbDiisWork& w, int n, double* c, double* g) {
@@ -97,41 +138,55 @@ __device__ inline double fg(const QbDiisWork& w, int n, double* c, double* g) {
     return f;
 }
 
-// Cholesky R^T R of the leading k x k block, upper R in place; nonzero on a non-positive pivot.
+// Cholesky R^T R of the leading k x k block (k <= 32), upper R in place, right-looking:
+// lane l owns column l.  Nonzero (the failing column + 1) on a non-positive pivot.
 __device__ inline int chol_upper(double* a, int ld, int k) {
+    const int l = lane_id();
+    __syncwarp();
     for (int j = 0; j < k; ++j) {
-        double s = 0.0;
-        for (int p = 0; p < j; ++p) {
-            double t = a[p + ld * j];
-            for (int q = 0; q < p; ++q) t -= a[q + ld * p] * a[q + ld * j];
-            t /= a[p + ld * p];
-            a[p + ld * j] = t;
-            s += t * t;
-        }
-        s = a[j + ld * j] - s;
-        if (s <= 0.0) return j + 1;
-        a[j + ld * j] = sqrt(s);
+        const double djj = a[j + ld * j];
+        if (djj <= 0.0) return j + 1;
+        const double rj = sqrt(djj), ri = 1.0 / rj;
+        const bool mine = l > j && l < k;
+        double ajl = 0.0;
+        if (mine) ajl = a[j + ld * l] * ri;
+        __syncwarp();
+        if (mine) a[j + ld * l] = ajl;
+        if (l == j) a[j + ld * j] = rj;
+        __syncwarp();
+        if (mine)
+            for (int i = j + 1; i <= l; ++i) a[i + ld * l] = fma(-a[j + ld * i], ajl, a[i + ld * l]);
+        __syncwarp();
     }
     return 0;
 }
 
-// R^T x = b (trans) or R x = b, R upper k x k in place of b; nonzero on a zero pivot.
+// R^T x = b (trans) or R x = b, R upper k x k (k <= 32), in place of b; lane l owns b_l.
+// Nonzero (the first zero pivot + 1) on a zero pivot.
 __device__ inline int tri_solve(const double* r, int ld, int k, double* b, bool trans) {
-    for (int i = 0; i < k; ++i)
-        if (r[i + ld * i] == 0.0) return i + 1;
+    const int l = lane_id();
+    __syncwarp();
+    const double dl = l < k ? r[l + ld * l] : 1.0;
+    const unsigned zero = __ballot_sync(kFull, l < k && dl == 0.0);
+    if (zero) return __ffs(zero);
+    const double rl = 1.0 / dl;
+    double bl = l < k ? b[l] : 0.0;
     if (trans) {
         for (int i = 0; i < k; ++i) {
-            double t = b[i];
-            for (int p = 0; p < i; ++p) t -= r[p + ld * i] * b[p];
-            b[i] = t / r[i + ld * i];
+            if (l == i) bl *= rl;
+            const double bi = __shfl_sync(kFull, bl, i);
+            if (l > i && l < k) bl = fma(-r[i + ld * l], bi, bl);
         }
     } else {
         for (int i = k - 1; i >= 0; --i) {
-            double t = b[i];
-            for (int p = i + 1; p < k; ++p) t -= r[i + ld * p] * b[p];
-            b[i] = t / r[i + ld * i];
+            if (l == i) bl *= rl;
+            const double bi = __shfl_sync(kFull, bl, i);
+            if (l < i) bl = fma(-r[l + ld * i], bi, bl);
         }
     }
+    __syncwarp();
+    if (l < k) b[l] = bl;
+    __syncwarp();
     return 0;
 }
 
@@ -265,15 +320,15 @@ __device__ inline int search_step(Search& S, bool start, double f, double g, dou
 }
 
 // L-BFGS-B over n variables, each either free (bounded = false) or with lower bound 0.
+// The correction pairs sit in the columns of ws / wy in a ring (slot(k) = (head + k) mod m).
 struct Lbfgsb {
     QbDiisWork& w;
     int n;
     bool bounded;
-    int col, head, tail, iupdat;
+    int col, head, tail, iupdat, nfree;
     double theta;
-    bool updated;
 
-    __device__ Lbfgsb(QbDiisWork& w_, int n_, bool b) : w(w_), n(n_), bounded(b) { refresh(); }
+    __device__ Lbfgsb(QbDiisWork& w_, int n_, bool b) : w(w_), n(n_), bounded(b), nfree(0) { refresh(); }
 
     __device__ void refresh() {
         col = 0;
@@ -281,192 +336,142 @@ struct Lbfgsb {
         tail = 0;
         iupdat = 0;
         theta = 1.0;
-        updated = false;
     }
     __device__ int slot(int k) const { return (head + k) % QB_DS_M; }
-    __device__ double& WS(int i, int k) { return w.ws[i + QB_DS_N * slot(k)]; }
-    __device__ double& WY(int i, int k) { return w.wy[i + QB_DS_N * slot(k)]; }
+    __device__ const double* ycol(int k) const { return w.wy + QB_DS_N * slot(k); }
+    __device__ const double* scol(int k) const { return w.ws + QB_DS_N * slot(k); }
     __device__ double& SY(int i, int j) { return w.sy[i + QB_DS_M * j]; }
     __device__ double& SS(int i, int j) { return w.ss[i + QB_DS_M * j]; }
 
+    // infinity norm of the projected gradient
     __device__ double pg_norm(const double* x, const double* g) const {
-        double s = 0.0;
-        for (int i = 0; i < n; ++i) {
-            double gi = g[i];
-            if (bounded && gi >= 0) gi = fmin(x[i], gi);   // lower bound 0
-            s = fmax(s, fabs(gi));
+        const int l = lane_id();
+        double gi = 0.0;
+        if (l < n) {
+            gi = g[l];
+            if (bounded && gi >= 0) gi = fmin(x[l], gi);   // lower bound 0
         }
-        return s;
+        return wmax(fabs(gi));
     }
 
     // p = M v (compact representation's middle matrix), v and p of length 2 col.
     __device__ int middle(const double* v, double* p) {
         if (col == 0) return 0;
-        p[col] = v[col];
-        for (int i = 1; i < col; ++i) {
+        const int l = lane_id();
+        __syncwarp();
+        if (l < col) {
             double sum = 0.0;
-            for (int k = 0; k < i; ++k) sum += SY(i, k) * v[k] / SY(k, k);
-            p[col + i] = v[col + i] + sum;
+            for (int k = 0; k < l; ++k) sum = fma(SY(l, k) * v[k], w.dinv[k], sum);
+            p[col + l] = v[col + l] + sum;
         }
         if (tri_solve(w.wt, QB_DS_M, col, p + col, true)) return -1;
-        for (int i = 0; i < col; ++i) p[i] = v[i] / sqrt(SY(i, i));
+        if (l < col) p[l] = v[l] * w.sqinv[l];
         if (tri_solve(w.wt, QB_DS_M, col, p + col, false)) return -1;
-        for (int i = 0; i < col; ++i) p[i] = -p[i] / sqrt(SY(i, i));
-        for (int i = 0; i < col; ++i) {
+        if (l < col) p[l] = -p[l] * w.sqinv[l];
+        __syncwarp();
+        if (l < col) {
             double sum = 0.0;
-            for (int k = i + 1; k < col; ++k) sum += SY(k, i) * p[col + k] / SY(i, i);
-            p[i] += sum;
+            for (int k = l + 1; k < col; ++k) sum = fma(SY(k, l), p[col + k], sum);
+            p[l] += sum * w.dinv[l];
         }
+        __syncwarp();
         return 0;
     }
 
-    __device__ static void heap_pop(int cnt, double* t, int* ord, bool build) {
-        if (build) {
-            for (int k = 1; k < cnt; ++k) {
-                const double val = t[k];
-                const int idx = ord[k];
-                int i = k;
-                while (i > 0) {
-                    const int j = (i + 1) / 2 - 1;
-                    if (!(val < t[j])) break;
-                    t[i] = t[j];
-                    ord[i] = ord[j];
-                    i = j;
-                }
-                t[i] = val;
-                ord[i] = idx;
-            }
-        }
-        if (cnt > 1) {
-            const double out = t[0];
-            const int oidx = ord[0];
-            const double val = t[cnt - 1];
-            const int idx = ord[cnt - 1];
-            int i = 0;
-            while (true) {
-                int j = 2 * (i + 1) - 1;
-                if (j > cnt - 2) break;
-                if (t[j + 1] < t[j]) j = j + 1;
-                if (!(t[j] < val)) break;
-                t[i] = t[j];
-                ord[i] = ord[j];
-                i = j;
-            }
-            t[i] = val;
-            ord[i] = idx;
-            t[cnt - 1] = out;
-            ord[cnt - 1] = oidx;
-        }
-    }
-
-    // Generalised Cauchy point: z and c = W^T (z - x); updates where[].
+    // Generalised Cauchy point xcp and c = W^T (xcp - x); updates where[].  The breakpoints
+    // are visited in increasing order by a warp minimum over the lanes still to be visited
+    // (equal breakpoints in increasing variable order).
     __device__ int cauchy(const double* x, const double* g, double* xcp, double* c) {
-        const int col2 = 2 * col;
-        for (int i = 0; i < n; ++i) xcp[i] = x[i];
+        const int l = lane_id(), col2 = 2 * col;
+        const bool own = l < n;
+        const double xl = own ? x[l] : 0.0, gl = own ? g[l] : 0.0;
+        if (own) xcp[l] = xl;
+        __syncwarp();
         if (pg_norm(x, g) <= 0.0) return 0;
-        bool bnded = true;
-        int nfree = n, nbreak = 0, ibkmin = 0;
-        double bkmin = 0.0, f1 = 0.0, tl = 0.0;
+        const double neggi = -gl;
+        int wh = own ? w.where[l] : -2;
+        if (own && wh != -1) {   // bounded variable (lower bound 0)
+            wh = 0;
+            if (xl <= 0) {
+                if (neggi <= 0) wh = 1;
+            } else if (fabs(neggi) <= 0) {
+                wh = -3;
+            }
+        }
+        const bool moving = own && (wh == 0 || wh == -1);
+        double dl = moving ? neggi : 0.0;
+        double f1 = -wsum(moving ? neggi * neggi : 0.0);
+        const bool brk = moving && bounded && neggi < 0;
+        const bool fre = moving && !brk;
+        double my_tb = brk ? xl / (-neggi) : INFINITY;
+        const int nbreak = __popc(__ballot_sync(kFull, brk));
+        const int nfree0 = n - __popc(__ballot_sync(kFull, fre));
+        const bool bnded = !wany(fre && fabs(neggi) > 0);
+        if (own) {
+            w.d[l] = dl;
+            w.where[l] = wh;
+        }
+        __syncwarp();
         double* p = w.p;
         double* v = w.vv;
         double* wbp = w.wbp;
-        double* d = w.d;
-        for (int j = 0; j < col2; ++j) p[j] = 0.0;
-        for (int i = 0; i < n; ++i) {
-            const double neggi = -g[i];
-            if (w.where[i] != -1) {   // bounded variable (lower bound 0)
-                tl = x[i];
-                w.where[i] = 0;
-                if (tl <= 0) {
-                    if (neggi <= 0) w.where[i] = 1;
-                } else if (fabs(neggi) <= 0) {
-                    w.where[i] = -3;
-                }
-            }
-            if (w.where[i] != 0 && w.where[i] != -1) {
-                d[i] = 0.0;
-            } else {
-                d[i] = neggi;
-                f1 -= neggi * neggi;
-                for (int j = 0; j < col; ++j) {
-                    p[j] += WY(i, j) * neggi;
-                    p[col + j] += WS(i, j) * neggi;
-                }
-                if (bounded && neggi < 0) {
-                    w.ord[nbreak] = i;
-                    w.tb[nbreak] = tl / (-neggi);
-                    if (nbreak == 0 || w.tb[nbreak] < bkmin) { bkmin = w.tb[nbreak]; ibkmin = nbreak; }
-                    ++nbreak;
-                } else {
-                    --nfree;
-                    w.ord[nfree] = i;
-                    if (fabs(neggi) > 0) bnded = false;
-                }
-            }
+        if (l < col2) {   // p = W^T d
+            const double* src = l < col ? ycol(l) : scol(l - col);
+            double s = 0.0;
+            for (int i = 0; i < n; ++i) s = fma(src[i], w.d[i], s);
+            if (l >= col) s *= theta;
+            p[l] = s;
         }
-        if (theta != 1.0)
-            for (int j = 0; j < col; ++j) p[col + j] *= theta;
-        if (nbreak == 0 && nfree == n) return 0;
-        for (int j = 0; j < 2 * QB_DS_M; ++j) c[j] = 0.0;
+        __syncwarp();
+        if (nbreak == 0 && nfree0 == n) return 0;
+        if (l < 2 * QB_DS_M) c[l] = 0.0;
         double f2 = -theta * f1;
         const double f2_org = f2;
         if (col > 0) {
             if (middle(p, v)) return -1;
-            double pv = 0.0;
-            for (int j = 0; j < col2; ++j) pv += v[j] * p[j];
-            f2 -= pv;
+            f2 -= wsum(l < col2 ? v[l] * p[l] : 0.0);
         }
         double dtm = -f1 / f2, tsum = 0.0;
+        double cl = 0.0, pl = l < col2 ? p[l] : 0.0;   // lane l owns c[l], p[l]
         if (nbreak > 0) {
-            int nleft = nbreak, it = 1;
+            int nleft = nbreak;
             double tj = 0.0;
             for (int guard = 0; guard <= QB_DS_N; ++guard) {
                 const double tj0 = tj;
                 int ibp;
-                if (it == 1) {
-                    tj = bkmin;
-                    ibp = w.ord[ibkmin];
-                } else {
-                    if (it == 2 && ibkmin != nbreak - 1) {
-                        w.tb[ibkmin] = w.tb[nbreak - 1];
-                        w.ord[ibkmin] = w.ord[nbreak - 1];
-                    }
-                    heap_pop(nleft, w.tb, w.ord, it == 2);
-                    tj = w.tb[nleft - 1];
-                    ibp = w.ord[nleft - 1];
-                }
+                tj = wargmin(my_tb, ibp);
                 const double dt = tj - tj0;
                 if (dtm < dt) break;
                 tsum += dt;
                 --nleft;
-                ++it;
-                const double dibp = d[ibp];
-                d[ibp] = 0.0;
-                const double zibp = -x[ibp];   // to the lower bound 0
-                xcp[ibp] = 0.0;
-                w.where[ibp] = 1;
+                const double dibp = __shfl_sync(kFull, dl, ibp);
+                const double zibp = -__shfl_sync(kFull, xl, ibp);   // to the lower bound 0
+                if (l == ibp) {
+                    my_tb = INFINITY;
+                    dl = 0.0;
+                    wh = 1;
+                    xcp[l] = 0.0;
+                    w.where[l] = 1;
+                }
                 if (nleft == 0 && nbreak == n) {   // every variable fixed
-                    if (col > 0)
-                        for (int j = 0; j < col2; ++j) c[j] += dt * p[j];
+                    if (col > 0 && l < col2) c[l] = fma(dt, pl, cl);
+                    __syncwarp();
                     return 0;
                 }
                 const double dibp2 = dibp * dibp;
                 f1 = f1 + dt * f2 + dibp2 - theta * dibp * zibp;
                 f2 = f2 - theta * dibp2;
                 if (col > 0) {
-                    for (int j = 0; j < col2; ++j) c[j] += dt * p[j];
-                    for (int j = 0; j < col; ++j) {
-                        wbp[j] = WY(ibp, j);
-                        wbp[col + j] = theta * WS(ibp, j);
+                    cl = fma(dt, pl, cl);
+                    if (l < col2) {
+                        c[l] = cl;
+                        wbp[l] = l < col ? ycol(l)[ibp] : theta * scol(l - col)[ibp];
                     }
                     if (middle(wbp, v)) return -1;
-                    double wmc = 0, wmp = 0, wmw = 0;
-                    for (int j = 0; j < col2; ++j) {
-                        wmc += c[j] * v[j];
-                        wmp += p[j] * v[j];
-                        wmw += wbp[j] * v[j];
-                    }
-                    for (int j = 0; j < col2; ++j) p[j] -= dibp * wbp[j];
+                    const double vl = l < col2 ? v[l] : 0.0, wl = l < col2 ? wbp[l] : 0.0;
+                    const double wmc = wsum(cl * vl), wmp = wsum(pl * vl), wmw = wsum(wl * vl);
+                    pl = fma(-dibp, wl, pl);
+                    if (l < col2) p[l] = pl;
                     f1 += dibp * wmc;
                     f2 += 2.0 * dibp * wmp - dibp2 * wmw;
                 }
@@ -487,151 +492,170 @@ struct Lbfgsb {
         }
         if (dtm <= 0) dtm = 0;
         tsum += dtm;
-        for (int i = 0; i < n; ++i) xcp[i] += tsum * d[i];
-        if (col > 0)
-            for (int j = 0; j < col2; ++j) c[j] += dtm * p[j];
+        __syncwarp();
+        if (own) {
+            xcp[l] = fma(tsum, dl, xcp[l]);
+            w.d[l] = dl;
+        }
+        if (col > 0 && l < col2) c[l] = fma(dtm, pl, cl);
+        __syncwarp();
         return 0;
     }
 
+    // freel = the variables with where <= 0 in increasing order; nfree their count
     __device__ void collect_free() {
-        w.nfree = 0;
-        w.nact = 0;
-        for (int i = 0; i < n; ++i) {
-            if (w.where[i] <= 0) w.freel[w.nfree++] = i;
-            else w.actl[w.nact++] = i;
-        }
+        const int l = lane_id();
+        const bool fr = l < n && w.where[l] <= 0;
+        const unsigned fm = __ballot_sync(kFull, fr);
+        if (fr) w.freel[__popc(fm & ((1u << l) - 1u))] = l;
+        nfree = __popc(fm);
+        __syncwarp();
     }
 
-    // LEL^T factor of K = [-D - Y'ZZ'Y/theta, L_a' - R_z'; L_a - R_z, theta S'AA'S] into wn.
+    // LEL^T factor of K = [-D - Y'ZZ'Y/theta, L_a' - R_z'; L_a - R_z, theta S'AA'S] into wn
+    // (Z: free variables, A: active ones).
     __device__ int form_k() {
-        const int ld = 2 * QB_DS_M;
+        const int ld = 2 * QB_DS_M, l = lane_id();
         double* wn = w.wn;
-        for (int i = 0; i < ld * ld; ++i) wn[i] = 0.0;
-        for (int iy = 0; iy < col; ++iy)
-            for (int jy = 0; jy <= iy; ++jy) {
-                double yzzy = 0, saas = 0;
-                for (int q = 0; q < w.nfree; ++q) {
-                    const int k = w.freel[q];
-                    yzzy += WY(k, iy) * WY(k, jy);
-                }
-                for (int q = 0; q < w.nact; ++q) {
-                    const int k = w.actl[q];
-                    saas += WS(k, iy) * WS(k, jy);
-                }
-                wn[jy + ld * iy] = yzzy / theta;
+        for (int i = l; i < ld * ld; i += 32) wn[i] = 0.0;
+        __syncwarp();
+        for (int e = l; e < col * col; e += 32) {
+            const int jy = e % col, iy = e / col;
+            const double *yi = ycol(iy), *yj = ycol(jy), *si = scol(iy);
+            const double* sj = scol(jy);
+            const bool upper = jy <= iy, strict = jy < iy;
+            double yzzy = 0, saas = 0, cross = 0;
+            for (int k = 0; k < n; ++k) {
+                const bool fr = w.where[k] <= 0;
+                yzzy = fma(fr ? yi[k] : 0.0, yj[k], yzzy);
+                saas = fma(fr ? 0.0 : si[k], sj[k], saas);
+                cross = fma((strict != fr) ? si[k] : 0.0, yj[k], cross);
+            }
+            if (upper) {
+                wn[jy + ld * iy] = yzzy / theta + (jy == iy ? SY(iy, iy) : 0.0);
                 wn[(col + jy) + ld * (col + iy)] = saas * theta;
             }
-        for (int iy = 0; iy < col; ++iy) {
-            wn[iy + ld * iy] += SY(iy, iy);
-            for (int jy = 0; jy < col; ++jy) {
-                double val = 0;
-                if (jy < iy) {
-                    for (int q = 0; q < w.nact; ++q) {
-                        const int k = w.actl[q];
-                        val += WS(k, iy) * WY(k, jy);
-                    }
-                    val = -val;
-                } else {
-                    for (int q = 0; q < w.nfree; ++q) {
-                        const int k = w.freel[q];
-                        val += WS(k, iy) * WY(k, jy);
-                    }
-                }
-                wn[jy + ld * (col + iy)] = val;
-            }
+            wn[jy + ld * (col + iy)] = strict ? -cross : cross;
         }
         if (chol_upper(wn, ld, col)) return -1;
-        for (int js = col; js < 2 * col; ++js)
-            if (tri_solve(wn, ld, col, wn + ld * js, true)) return -1;
-        for (int is = col; is < 2 * col; ++is)
-            for (int js = is; js < 2 * col; ++js) {
-                double s = 0;
-                for (int k = 0; k < col; ++k) s += wn[k + ld * is] * wn[k + ld * js];
-                wn[is + ld * js] += s;
+        // columns col .. 2 col - 1 of the top block rows: R^T X = B, one column per lane
+        {
+            const double dl = l < col ? wn[l + ld * l] : 1.0;
+            if (wany(l < col && dl == 0.0)) return -1;
+            if (l < col) w.rinv[l] = 1.0 / dl;
+            __syncwarp();
+            if (l < col) {
+                double* bcol = wn + ld * (col + l);
+                for (int i = 0; i < col; ++i) {
+                    double t = bcol[i];
+                    for (int q = 0; q < i; ++q) t = fma(-wn[q + ld * i], bcol[q], t);
+                    bcol[i] = t * w.rinv[i];
+                }
             }
+            __syncwarp();
+        }
+        for (int e = l; e < col * col; e += 32) {
+            const int a = e % col, b = e / col;
+            if (a <= b) {
+                const double *ca = wn + ld * (col + a), *cb = wn + ld * (col + b);
+                double s = 0;
+                for (int k = 0; k < col; ++k) s = fma(ca[k], cb[k], s);
+                wn[(col + a) + ld * (col + b)] += s;
+            }
+        }
         if (chol_upper(wn + col + ld * col, ld, col)) return -2;
         return 0;
     }
 
+    // T = theta S'S + L D^-1 L', factored; also the reciprocals of SY's diagonal.
     __device__ int form_t() {
-        for (int j = 0; j < col; ++j) w.wt[QB_DS_M * j] = theta * SS(0, j);
-        for (int i = 1; i < col; ++i)
-            for (int j = i; j < col; ++j) {
+        const int l = lane_id();
+        if (l < col) {
+            const double dk = SY(l, l);
+            w.dinv[l] = 1.0 / dk;
+            w.sqinv[l] = 1.0 / sqrt(dk);
+        }
+        __syncwarp();
+        for (int e = l; e < col * col; e += 32) {
+            const int i = e % col, j = e / col;
+            if (i <= j) {
                 double s = 0;
-                for (int k = 0; k < i; ++k) s += SY(i, k) * SY(j, k) / SY(k, k);
-                w.wt[i + QB_DS_M * j] = s + theta * SS(i, j);
+                for (int k = 0; k < i; ++k) s = fma(SY(i, k) * SY(j, k), w.dinv[k], s);
+                w.wt[i + QB_DS_M * j] = (i == 0) ? theta * SS(0, j) : s + theta * SS(i, j);
             }
+        }
         return chol_upper(w.wt, QB_DS_M, col) ? -3 : 0;
     }
 
-    // r = -Z^T (B (z - x) + g) over the free variables.
+    // r = -Z^T (B (z - x) + g) over the free variables (r indexed by the free list).
     __device__ int reduced_gradient(const double* x, const double* g, const double* z, const double* c, double* r) {
+        const int l = lane_id();
         if (!bounded && col > 0) {
-            for (int i = 0; i < n; ++i) r[i] = -g[i];
+            if (l < n) r[l] = -g[l];
+            __syncwarp();
             return 0;
-        }
-        for (int q = 0; q < w.nfree; ++q) {
-            const int k = w.freel[q];
-            r[q] = -theta * (z[k] - x[k]) - g[k];
         }
         double* a = w.wv;
         if (middle(c, a)) return -8;
-        for (int j = 0; j < col; ++j) {
-            const double a1 = a[j], a2 = theta * a[col + j];
-            for (int q = 0; q < w.nfree; ++q) {
-                const int k = w.freel[q];
-                r[q] += WY(k, j) * a1 + WS(k, j) * a2;
+        if (l < nfree) {
+            const int k = w.freel[l];
+            double rq = -theta * (z[k] - x[k]) - g[k];
+            for (int j = 0; j < col; ++j) {
+                const double a1 = a[j], a2 = theta * a[col + j];
+                rq += ycol(j)[k] * a1 + scol(j)[k] * a2;
             }
+            r[l] = rq;
         }
+        __syncwarp();
         return 0;
     }
 
-    // Subspace Newton step from the Cauchy point z (in place), projection, backtracking.
+    // Subspace Newton step from the Cauchy point x (= z, in place), projection, backtracking;
+    // d holds the reduced gradient over the free list on entry.
     __device__ int subspace_min(const double* xx, const double* gg, double* x, double* d) {
-        const int ld = 2 * QB_DS_M, nsub = w.nfree;
+        const int ld = 2 * QB_DS_M, nsub = nfree, l = lane_id(), col2 = 2 * col;
         double* wv = w.wv;
-        for (int i = 0; i < col; ++i) {
-            double t1 = 0, t2 = 0;
-            for (int j = 0; j < nsub; ++j) {
-                const int k = w.freel[j];
-                t1 += WY(k, i) * d[j];
-                t2 += WS(k, i) * d[j];
-            }
-            wv[i] = t1;
-            wv[col + i] = theta * t2;
+        if (l < col2) {
+            const double* src = l < col ? ycol(l) : scol(l - col);
+            double t = 0;
+            for (int j = 0; j < nsub; ++j) t = fma(src[w.freel[j]], d[j], t);
+            wv[l] = l < col ? t : theta * t;
         }
-        if (tri_solve(w.wn, ld, 2 * col, wv, true)) return -1;
-        for (int i = 0; i < col; ++i) wv[i] = -wv[i];
-        if (tri_solve(w.wn, ld, 2 * col, wv, false)) return -1;
-        for (int jy = 0; jy < col; ++jy)
-            for (int i = 0; i < nsub; ++i) {
-                const int k = w.freel[i];
-                d[i] += WY(k, jy) * wv[jy] / theta + WS(k, jy) * wv[col + jy];
-            }
-        for (int i = 0; i < nsub; ++i) d[i] /= theta;
-        double* xp = w.xp;
-        for (int i = 0; i < n; ++i) xp[i] = x[i];
-        bool hit = false;
-        for (int i = 0; i < nsub; ++i) {
-            const int k = w.freel[i];
-            if (!bounded) {
-                x[k] = x[k] + d[i];
-            } else {
-                x[k] = fmax(0.0, x[k] + d[i]);
-                if (x[k] == 0.0) hit = true;
-            }
+        if (tri_solve(w.wn, ld, col2, wv, true)) return -1;
+        if (l < col) wv[l] = -wv[l];
+        if (tri_solve(w.wn, ld, col2, wv, false)) return -1;
+        if (l < col) wv[l] /= theta;
+        __syncwarp();
+        if (l < nsub) {
+            const int k = w.freel[l];
+            double dq = d[l];
+            for (int jy = 0; jy < col; ++jy) dq += ycol(jy)[k] * wv[jy] + scol(jy)[k] * wv[col + jy];
+            d[l] = dq / theta;
         }
-        if (!hit) return 0;
-        double ddp = 0;
-        for (int i = 0; i < n; ++i) ddp += (x[i] - xx[i]) * gg[i];
+        if (l < n) w.xp[l] = x[l];
+        __syncwarp();
+        bool hitl = false;
+        if (l < nsub) {
+            const int k = w.freel[l];
+            double nx = x[k] + d[l];
+            if (bounded) {
+                nx = fmax(0.0, nx);
+                hitl = nx == 0.0;
+            }
+            x[k] = nx;
+        }
+        __syncwarp();
+        if (!wany(hitl)) return 0;
+        const double ddp = wsum(l < n ? (x[l] - xx[l]) * gg[l] : 0.0);
         if (ddp <= 0) return 0;
-        for (int i = 0; i < n; ++i) x[i] = xp[i];
+        if (l < n) x[l] = w.xp[l];
+        __syncwarp();
+        // the longest feasible step along d (every lane walks the free list alike)
         double alpha = 1.0, temp1 = alpha;
         int ibd = -1;
         for (int i = 0; i < nsub; ++i) {
             const int k = w.freel[i];
             const double dk = d[i];
-            if (!bounded) continue;
             if (dk < 0) {
                 const double t2 = -x[k];
                 if (t2 >= 0) temp1 = 0;
@@ -642,15 +666,20 @@ struct Lbfgsb {
                 ibd = i;
             }
         }
-        if (alpha < 1.0 && ibd >= 0 && d[ibd] < 0) {
+        const bool pin = alpha < 1.0 && ibd >= 0 && d[ibd] < 0;
+        __syncwarp();
+        if (pin && l == 0) {
             x[w.freel[ibd]] = 0.0;
             d[ibd] = 0;
         }
-        for (int i = 0; i < nsub; ++i) x[w.freel[i]] += alpha * d[i];
+        __syncwarp();
+        if (l < nsub) x[w.freel[l]] += alpha * d[l];
+        __syncwarp();
         return 0;
     }
 
     __device__ void update_memory(const double* s, const double* y, double rr, double dr, double stp, double dtd) {
+        const int l = lane_id();
         if (iupdat <= QB_DS_M) {
             col = iupdat;
             tail = (head + iupdat - 1) % QB_DS_M;
@@ -658,60 +687,78 @@ struct Lbfgsb {
             tail = (tail + 1) % QB_DS_M;
             head = (head + 1) % QB_DS_M;
         }
-        for (int i = 0; i < n; ++i) {
-            w.ws[i + QB_DS_N * tail] = s[i];
-            w.wy[i + QB_DS_N * tail] = y[i];
+        if (l < n) {
+            w.ws[l + QB_DS_N * tail] = s[l];
+            w.wy[l + QB_DS_N * tail] = y[l];
         }
         theta = rr / dr;
-        if (iupdat > QB_DS_M) {
-            for (int j = 0; j < col - 1; ++j) {
-                for (int i = 0; i <= j; ++i) SS(i, j) = SS(i + 1, j + 1);
-                for (int i = j; i < col - 1; ++i) SY(i, j) = SY(i + 1, j + 1);
+        if (iupdat > QB_DS_M) {   // drop the oldest pair: shift SS (upper) and SY (lower) up-left
+            const int c1 = col - 1;
+            double* tmp = w.wn;   // free until the next form_k
+            for (int e = l; e < c1 * c1; e += 32) {
+                const int i = e % c1, j = e / c1;
+                tmp[e] = (i <= j) ? SS(i + 1, j + 1) : 0.0;
+                tmp[c1 * c1 + e] = (i >= j) ? SY(i + 1, j + 1) : 0.0;
+            }
+            __syncwarp();
+            for (int e = l; e < c1 * c1; e += 32) {
+                const int i = e % c1, j = e / c1;
+                if (i <= j) SS(i, j) = tmp[e];
+                if (i >= j) SY(i, j) = tmp[c1 * c1 + e];
             }
         }
-        for (int j = 0; j < col - 1; ++j) {
+        __syncwarp();
+        if (l < col - 1) {
+            const double *yj = ycol(l), *sj = scol(l);
             double a = 0, b = 0;
             for (int i = 0; i < n; ++i) {
-                a += s[i] * WY(i, j);
-                b += WS(i, j) * s[i];
+                a = fma(s[i], yj[i], a);
+                b = fma(sj[i], s[i], b);
             }
-            SY(col - 1, j) = a;
-            SS(j, col - 1) = b;
+            SY(col - 1, l) = a;
+            SS(l, col - 1) = b;
         }
-        SS(col - 1, col - 1) = (stp == 1.0) ? dtd : stp * stp * dtd;
-        SY(col - 1, col - 1) = dr;
+        if (l == 0) {
+            SS(col - 1, col - 1) = (stp == 1.0) ? dtd : stp * stp * dtd;
+            SY(col - 1, col - 1) = dr;
+        }
+        __syncwarp();
     }
 
     // Minimise from w.x (in place); factr 1e5, pgtol 1e-15, 10000 iterations / evaluations.
     __device__ int run() {
         const double tol = 1e5 * kEps, pgtol = 1e-15;
         const int maxiter = 10000, maxfun = 10000;
+        const int l = lane_id();
+        const bool own = l < n;
         double *x = w.x, *g = w.g, *z = w.z, *d = w.d, *r = w.r, *xs = w.xs, *gs = w.gs;
-        for (int i = 0; i < n; ++i) {
-            if (bounded && x[i] < 0.0) x[i] = 0.0;
-            w.where[i] = bounded ? 0 : -1;
+        if (own) {
+            if (bounded && x[l] < 0.0) x[l] = 0.0;
+            w.where[l] = bounded ? 0 : -1;
         }
-        w.nfree = 0;
-        w.nact = 0;
+        nfree = 0;
+        __syncwarp();
         double f = fg(w, n, x, g);
         int nfgv = 1, iter = 0;
         if (pg_norm(x, g) <= pgtol) return iter;
         for (int outer = 0; outer < 4 * maxiter; ++outer) {
             if (!bounded && col > 0) {
-                for (int i = 0; i < n; ++i) z[i] = x[i];
+                if (own) z[l] = x[l];
+                __syncwarp();
             } else {
                 if (cauchy(x, g, z, w.cw) != 0) { refresh(); continue; }
                 collect_free();
             }
-            if (w.nfree > 0 && col > 0) {
+            if (nfree > 0 && col > 0) {
                 if (form_k() != 0) { refresh(); continue; }
                 if (reduced_gradient(x, g, z, w.cw, r) != 0) { refresh(); continue; }
                 if (subspace_min(x, g, z, r) != 0) { refresh(); continue; }
             }
-            for (int i = 0; i < n; ++i) d[i] = z[i] - x[i];
-            double dtd = 0.0;
-            for (int i = 0; i < n; ++i) dtd += d[i] * d[i];
+            double dl = own ? z[l] - x[l] : 0.0;
+            if (own) d[l] = dl;
+            const double dtd = wsum(dl * dl);
             const double dnorm = sqrt(dtd);
+            __syncwarp();
             double stpmx = 1e10;
             if (bounded) {
                 if (iter == 0) {
@@ -728,9 +775,10 @@ struct Lbfgsb {
                 }
             }
             double stp = (iter == 0) ? fmin(1.0 / dnorm, stpmx) : 1.0;
-            for (int i = 0; i < n; ++i) {
-                xs[i] = x[i];
-                gs[i] = g[i];
+            const double xl0 = own ? x[l] : 0.0, gl0 = own ? g[l] : 0.0;
+            if (own) {
+                xs[l] = xl0;
+                gs[l] = gl0;
             }
             const double fold = f;
             int ifun = 0, iback = 0;
@@ -738,8 +786,7 @@ struct Lbfgsb {
             Search S;
             bool newx = false, start = true;
             for (int ls = 0; ls < 64; ++ls) {
-                gd = 0.0;
-                for (int i = 0; i < n; ++i) gd += g[i] * d[i];
+                gd = wsum(own ? g[l] * dl : 0.0);
                 if (ifun == 0) {
                     gdold = gd;
                     if (gd >= 0) break;   // not a descent direction
@@ -750,11 +797,9 @@ struct Lbfgsb {
                     ++ifun;
                     ++nfgv;
                     iback = ifun - 1;
-                    if (stp == 1.0) {
-                        for (int i = 0; i < n; ++i) x[i] = z[i];
-                    } else {
-                        for (int i = 0; i < n; ++i) x[i] = stp * d[i] + xs[i];
-                    }
+                    __syncwarp();
+                    if (own) x[l] = (stp == 1.0) ? z[l] : fma(stp, dl, xl0);
+                    __syncwarp();
                     if (iback >= 20) break;
                     f = fg(w, n, x, g);
                     continue;
@@ -763,10 +808,12 @@ struct Lbfgsb {
                 break;
             }
             if (!newx) {
-                for (int i = 0; i < n; ++i) {
-                    x[i] = xs[i];
-                    g[i] = gs[i];
+                __syncwarp();
+                if (own) {
+                    x[l] = xl0;
+                    g[l] = gl0;
                 }
+                __syncwarp();
                 f = fold;
                 if (col == 0) return iter + 1;
                 refresh();
@@ -778,25 +825,20 @@ struct Lbfgsb {
             if (sbgnrm <= pgtol) return iter;
             const double ddum0 = fmax(fmax(fabs(fold), fabs(f)), 1.0);
             if (fold - f <= tol * ddum0) return iter;
-            double rr = 0.0;
-            for (int i = 0; i < n; ++i) {
-                r[i] = g[i] - gs[i];
-                rr += r[i] * r[i];
-            }
+            const double rl = own ? g[l] - gl0 : 0.0;
+            if (own) r[l] = rl;
+            const double rr = wsum(rl * rl);
             double dr, ddum;
             if (stp == 1.0) {
                 dr = gd - gdold;
                 ddum = -gdold;
             } else {
                 dr = (gd - gdold) * stp;
-                for (int i = 0; i < n; ++i) d[i] *= stp;
+                if (own) d[l] = dl * stp;
                 ddum = -gdold * stp;
             }
-            if (dr <= kEps * ddum) {
-                updated = false;
-                continue;
-            }
-            updated = true;
+            __syncwarp();
+            if (dr <= kEps * ddum) continue;
             ++iupdat;
             update_memory(d, r, rr, dr, stp, dtd);
             if (form_t() != 0) { refresh(); continue; }
@@ -809,148 +851,178 @@ struct Lbfgsb {
 __device__ inline int spg(QbDiisWork& w, int n, bool bounded) {
     const double lmin = 1e-30, lmax = 1e30, gamma = 1e-4, sigma1 = 0.1, sigma2 = 0.9, eps = 1e-15;
     const int nitmax = 10000, nfevalmax = 10000, mem = 20;
-    double *x = w.x, *g = w.g, *xn = w.z, *gn = w.r, *dv = w.d;
-    auto pg_norm = [&](const double* xv, const double* gv) {
-        double s = 0.0;
-        for (int i = 0; i < n; ++i) {
-            double t = xv[i] - gv[i];
+    const int l = lane_id();
+    const bool own = l < n;
+    double *x = w.x, *g = w.g, *xn = w.z, *gn = w.r;
+    auto pg_norm = [&]() {
+        double t = 0.0;
+        if (own) {
+            t = x[l] - g[l];
             if (bounded) t = fmax(t, 0.0);
-            s = fmax(s, fabs(t - xv[i]));
+            t = fabs(t - x[l]);
         }
-        return s;
+        return wmax(t);
     };
-    if (bounded)
-        for (int i = 0; i < n; ++i) x[i] = fmax(x[i], 0.0);
+    if (bounded && own) x[l] = fmax(x[l], 0.0);
+    __syncwarp();
     double fc = obj_f(w, n, x);
     obj_g(w, n, x, g);
     int nfeval = 1, nit = 0;
-    double gnorm = pg_norm(x, g);
+    double gnorm = pg_norm();
     if (gnorm <= eps) return 0;
-    for (int i = 0; i < mem; ++i) w.fprev[i] = fc;
+    if (l < mem) w.fprev[l] = fc;
     double lam = fmin(lmax, fmax(lmin, 1.0 / gnorm));
     while (nit < nitmax) {
-        for (int i = 0; i < n; ++i) {
-            double t = x[i] - lam * g[i];
+        double dl = 0.0, xl = 0.0, gl = 0.0;
+        if (own) {
+            xl = x[l];
+            gl = g[l];
+            double t = xl - lam * gl;
             if (bounded) t = fmax(t, 0.0);
-            dv[i] = t - x[i];
+            dl = t - xl;
         }
-        double gtd = 0.0, fref = w.fprev[0];
-        for (int i = 0; i < n; ++i) gtd += g[i] * dv[i];
-        for (int i = 1; i < mem; ++i) fref = fmax(fref, w.fprev[i]);
+        const double gtd = wsum(gl * dl);
+        __syncwarp();
+        const double fref = wmax(l < mem ? w.fprev[l] : -INFINITY);
         double alpha = 1.0;
-        for (int i = 0; i < n; ++i) xn[i] = x[i] + alpha * dv[i];
+        if (own) xn[l] = fma(alpha, dl, xl);
+        __syncwarp();
         double fn = obj_f(w, n, xn);
         ++nfeval;
         while (fn > fref + gamma * alpha * gtd) {
             const double atemp = -0.5 * gtd * alpha * alpha / (fn - fc - alpha * gtd);
             if (atemp >= sigma1 && atemp <= sigma2 * alpha) alpha = atemp;
             else alpha /= 2;
-            for (int i = 0; i < n; ++i) xn[i] = x[i] + alpha * dv[i];
+            __syncwarp();
+            if (own) xn[l] = fma(alpha, dl, xl);
+            __syncwarp();
             fn = obj_f(w, n, xn);
             if (++nfeval > nfevalmax) {
-                for (int i = 0; i < n; ++i) x[i] = xn[i];
+                if (own) x[l] = xn[l];
+                __syncwarp();
                 return 2;
             }
         }
         ++nit;
-        w.fprev[nit % mem] = fn;
+        __syncwarp();
+        if (l == 0) w.fprev[nit % mem] = fn;
         obj_g(w, n, xn, gn);
-        double sts = 0, sty = 0;
-        for (int i = 0; i < n; ++i) {
-            const double s = xn[i] - x[i], y = gn[i] - g[i];
-            sts += s * s;
-            sty += s * y;
+        double s = 0.0, y = 0.0;
+        if (own) {
+            s = xn[l] - xl;
+            y = gn[l] - gl;
         }
+        const double sts = wsum(s * s), sty = wsum(s * y);
         lam = sty <= 0 ? lmax : fmin(lmax, fmax(lmin, sts / sty));
-        for (int i = 0; i < n; ++i) {
-            x[i] = xn[i];
-            g[i] = gn[i];
+        if (own) {
+            x[l] = xn[l];
+            g[l] = gn[l];
         }
+        __syncwarp();
         fc = fn;
-        gnorm = pg_norm(x, g);
+        gnorm = pg_norm();
         if (gnorm <= eps) return 0;
     }
     return 1;
 }
 
 // LU with partial pivoting of the leading n x n block of A (column-major, leading dimension
-// n), solving A x = b in place of b; returns the determinant (0 when a pivot vanishes).
+// n, n <= 32), solving A x = b in place of b; returns the determinant (0 when a pivot
+// vanishes).  Lane i owns row i in the elimination.
 __device__ inline double lu_solve(int n, double* A, double* b) {
+    const int l = lane_id();
     double det = 1.0;
+    __syncwarp();
     for (int k = 0; k < n; ++k) {
-        int p = k;
-        for (int i = k + 1; i < n; ++i)
-            if (fabs(A[i + n * k]) > fabs(A[p + n * k])) p = i;
+        const bool cand = l >= k && l < n;
+        const double a = cand ? fabs(A[l + n * k]) : -1.0;
+        const double mx = wmax(a);
+        const int p = __ffs(__ballot_sync(kFull, cand && a == mx)) - 1;   // first largest
         if (A[p + n * k] == 0.0) return 0.0;
+        __syncwarp();
         if (p != k) {
-            for (int j = 0; j < n; ++j) {
-                const double t = A[k + n * j];
-                A[k + n * j] = A[p + n * j];
-                A[p + n * j] = t;
+            if (l < n) {
+                const double t = A[k + n * l];
+                A[k + n * l] = A[p + n * l];
+                A[p + n * l] = t;
             }
-            const double t = b[k];
-            b[k] = b[p];
-            b[p] = t;
+            if (l == 0) {
+                const double t = b[k];
+                b[k] = b[p];
+                b[p] = t;
+            }
             det = -det;
+            __syncwarp();
         }
         const double pv = A[k + n * k];
         det *= pv;
-        for (int i = k + 1; i < n; ++i) {
-            const double f = A[i + n * k] / pv;
-            A[i + n * k] = f;
-            for (int j = k + 1; j < n; ++j) A[i + n * j] -= f * A[k + n * j];
-            b[i] -= f * b[k];
+        if (l > k && l < n) {
+            const double f = A[l + n * k] / pv;
+            A[l + n * k] = f;
+            for (int j = k + 1; j < n; ++j) A[l + n * j] = fma(-f, A[k + n * j], A[l + n * j]);
+            b[l] = fma(-f, b[k], b[l]);
         }
+        __syncwarp();
     }
+    const double rl = l < n ? 1.0 / A[l + n * l] : 0.0;
+    double bl = l < n ? b[l] : 0.0;
     for (int i = n - 1; i >= 0; --i) {
-        double t = b[i];
-        for (int j = i + 1; j < n; ++j) t -= A[i + n * j] * b[j];
-        b[i] = t / A[i + n * i];
+        if (l == i) bl *= rl;
+        const double bi = __shfl_sync(kFull, bl, i);
+        if (l < i) bl = fma(-A[l + n * i], bi, bl);
     }
+    __syncwarp();
+    if (l < n) b[l] = bl;
+    __syncwarp();
     return det;
 }
 
 }  // namespace qbds
 
-// CMsolver! (HartreeFock.jl:1445-1477) by one thread: solve [B 1; 1 0][c; l] = [-v; 1]; if
+// CMsolver! (HartreeFock.jl:1445-1477) by one warp: solve [B 1; 1 0][c; l] = [-v; 1]; if
 // `convex` and some c < 0, try the subsystems with index subsets removed (by increasing
 // size, smallest |c| first) until a non-negative solution appears; a singular bordered
 // matrix gets B += 4e-13 I (1000 getAtolVal).  B is m x m with leading dimension ldb, m <= 16.
 // Bounded: at most 64 perturbation rounds; returns false if they run out (c then holds the
-// last candidate).
+// last candidate).  Every lane walks the subsets alike; the LU solves are spread over lanes.
 static __device__ __noinline__ bool qb_cm_solve(QbDiisWork& w, int m, int convex, const double* Bin, int ldb,
                                                 const double* v, double* c) {
-    const int M = m + 1;
+    const int M = m + 1, l = qbds::lane_id();
     double *B = w.cmB, *A = w.cmA, *W = w.cmW, *b = w.cmb, *x = w.cmx;
-    for (int j = 0; j < m; ++j)
-        for (int i = 0; i < m; ++i) B[i + m * j] = Bin[i + ldb * j];
+    for (int e = l; e < m * m; e += 32) B[e] = Bin[(e % m) + ldb * (e / m)];
+    __syncwarp();
     for (int round = 0; round < 64; ++round) {
         for (int guard = 0; guard < 64; ++guard) {
-            for (int j = 0; j < M; ++j)
-                for (int i = 0; i < M; ++i)
-                    A[i + M * j] = (i < m && j < m) ? B[i + m * j] : ((i == m && j == m) ? 0.0 : 1.0);
-            for (int i = 0; i < M * M; ++i) W[i] = A[i];
-            for (int i = 0; i < M; ++i) x[i] = 0.0;
+            for (int e = l; e < M * M; e += 32) {
+                const int i = e % M, j = e / M;
+                const double a = (i < m && j < m) ? B[i + m * j] : ((i == m && j == m) ? 0.0 : 1.0);
+                A[e] = a;
+                W[e] = a;
+            }
+            if (l < M) x[l] = 0.0;
             if (qbds::lu_solve(M, W, x) != 0.0) break;
-            for (int i = 0; i < m; ++i) B[i + m * i] += 4e-13;
+            if (l < m) B[l + m * l] += 4e-13;
+            __syncwarp();
         }
-        for (int i = 0; i < m; ++i) b[i] = v ? -v[i] : 0.0;
-        b[m] = 1.0;
-        for (int i = 0; i < M * M; ++i) W[i] = A[i];
-        for (int i = 0; i < M; ++i) x[i] = b[i];
+        if (l < m) b[l] = v ? -v[l] : 0.0;
+        if (l == m) b[l] = 1.0;
+        for (int e = l; e < M * M; e += 32) W[e] = A[e];
+        __syncwarp();
+        if (l < M) x[l] = b[l];
         qbds::lu_solve(M, W, x);
-        bool neg = false;
-        for (int i = 0; i < m; ++i) {
-            c[i] = x[i];
-            neg |= x[i] < 0.0;
+        const double xl = l < m ? x[l] : 0.0;
+        if (l < m) c[l] = xl;
+        const bool neg = qbds::wany(l < m && xl < 0.0);
+        if (!convex || !neg) {
+            __syncwarp();
+            return true;
         }
-        if (!convex || !neg) return true;
         int perm[QB_DS_N];
         for (int i = 0; i < m; ++i) perm[i] = i;
         for (int i = 1; i < m; ++i) {   // stable insertion sort by |c|
             const int t = perm[i];
             int j = i - 1;
-            while (j >= 0 && fabs(c[perm[j]]) > fabs(c[t])) {
+            while (j >= 0 && fabs(x[perm[j]]) > fabs(x[t])) {
                 perm[j + 1] = perm[j];
                 --j;
             }
@@ -965,16 +1037,19 @@ static __device__ __noinline__ bool qb_cm_solve(QbDiisWork& w, int m, int convex
                 int keep[QB_DS_N + 1], k = 0;
                 for (int i = 0; i <= m; ++i)
                     if (!(drop >> i & 1u)) keep[k++] = i;
-                for (int jj = 0; jj < k; ++jj) {
-                    x[jj] = b[keep[jj]];
-                    for (int ii = 0; ii < k; ++ii) W[ii + k * jj] = A[keep[ii] + M * keep[jj]];
+                __syncwarp();
+                if (l < k) {
+                    const int kl = keep[l];
+                    x[l] = b[kl];
+                    for (int jj = 0; jj < k; ++jj) W[l + k * jj] = A[kl + M * keep[jj]];
                 }
                 if (qbds::lu_solve(k, W, x) != 0.0) {
-                    bool bad = false;
-                    for (int i = 0; i < m; ++i) c[i] = 0.0;
-                    for (int jj = 0; jj < k - 1; ++jj) c[keep[jj]] = x[jj];
-                    for (int i = 0; i < m; ++i) bad |= c[i] < 0.0;
-                    if (!bad) return true;
+                    const double xk = l < k - 1 ? x[l] : 0.0;
+                    if (l < m) c[l] = 0.0;
+                    __syncwarp();
+                    if (l < k - 1) c[keep[l]] = xk;
+                    __syncwarp();
+                    if (!qbds::wany(l < k - 1 && xk < 0.0)) return true;
                 }
                 int pos = sz - 1;
                 while (pos >= 0 && comb[pos] == m - sz + pos) --pos;
@@ -983,22 +1058,25 @@ static __device__ __noinline__ bool qb_cm_solve(QbDiisWork& w, int m, int convex
                 for (int t = pos + 1; t < sz; ++t) comb[t] = comb[t - 1] + 1;
             }
         }
-        for (int i = 0; i < m; ++i) B[i + m * i] += 4e-13;
+        if (l < m) B[l + m * l] += 4e-13;
+        __syncwarp();
     }
     return false;
 }
 
-// One thread: solve the DIIS coefficient problem of m entries.  B (m x m, leading
-// dimension ldb) and v (m) describe it; c (m) is the starting point on entry and the
-// normalised coefficients on return.  solver: QB_DIIS_LBFGS or QB_DIIS_SPGB; convex adds
-// c >= 0.  Returns the solver's iteration count (L-BFGS-B) or status (SPG).
+// One warp: solve the DIIS coefficient problem of m entries.  B (m x m, leading dimension
+// ldb) and v (m) describe it; c (m) is the starting point on entry and the normalised
+// coefficients on return.  solver: QB_DIIS_LBFGS or QB_DIIS_SPGB; convex adds c >= 0.
+// Returns the solver's iteration count (L-BFGS-B) or status (SPG).
 static __device__ __noinline__ int qb_diis_iterative_solve(QbDiisWork& w, int solver, int convex, int m, const double* B,
-                                                    int ldb, const double* v, double* c) {
-    for (int j = 0; j < m; ++j) {
-        w.v[j] = v ? v[j] : 0.0;
-        for (int i = 0; i < m; ++i) w.B[i + QB_DS_N * j] = B[i + ldb * j];
-        w.x[j] = c[j];
+                                                           int ldb, const double* v, double* c) {
+    const int l = qbds::lane_id();
+    for (int e = l; e < m * m; e += 32) w.B[(e % m) + QB_DS_N * (e / m)] = B[(e % m) + ldb * (e / m)];
+    if (l < m) {
+        w.v[l] = v ? v[l] : 0.0;
+        w.x[l] = c[l];
     }
+    __syncwarp();
     int out;
     if (solver == QB_DIIS_SPGB) {
         out = qbds::spg(w, m, convex != 0);
@@ -1006,8 +1084,9 @@ static __device__ __noinline__ int qb_diis_iterative_solve(QbDiisWork& w, int so
         qbds::Lbfgsb opt(w, m, convex != 0);
         out = opt.run();
     }
-    w.iters = out;
+    if (l == 0) w.iters = out;
     const double s = qbds::shifted_sum(m, w.x);
-    for (int i = 0; i < m; ++i) c[i] = w.x[i] / s;
+    if (l < m) c[l] = w.x[l] / s;
+    __syncwarp();
     return out;
 }
