@@ -535,7 +535,7 @@ def batched_rhf(qb, n_mol, seed, cpu_seconds):
            "strategy": "SCFconfig((:DIIS,), (1e-10,), Dict(1=>[:solver=>:LCM])), RMS(dD) <= 1e-8, CoreH guess",
            "wall_s": wall, "ms_integrals": res.ms_integrals, "ms_scf": res.ms_scf,
            "mean_iterations_converged": float(res.iterations[conv].mean()) if conv.any() else None,
-           "graph_launches": res.graph_launches, "stored_quartets": res.quartets,
+           "graph_launches": res.graph_launches, "digest_chunk": res.digest_chunk, "stored_quartets": res.quartets,
            "stored_eri_gb": res.eri_doubles * 8 / 1e9,
            "eigensolver": "occupied subspace: Householder tridiagonalisation, FP32 Sturm bisection, "
                           "FP64 inverse iteration (one thread block per molecule)"}
