@@ -32,6 +32,12 @@ sys.path.insert(0, str(ROOT / "oracle"))
 
 METRIC = "ERI GQuartet/s (fused J+K build)"
 UNIT = "GQuartet/s"
+FLOPS_TABLE = Path(__file__).resolve().parent / "quiqbox.jl_gb300" / "csrc" / "flops_table.json"
+# DRAM bytes (read + write) of one launch of the dominant class kernel on the bench workload,
+# from one ncu capture of that kernel alone (dram__bytes_read.sum + dram__bytes_write.sum,
+# `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
+#  --kernel-name-base demangled -k regex:<kernel> -c 1 python bench.py --jk-only 1`)
+DOMINANT_TRAFFIC = {}
 WORKLOAD = "ERI+J/K: 64 H + 16 C/N/O in a 14 bohr cube, 3-prim Cartesian s/p/d shells, N=416, FP64, Schwarz 1e-12"
 L2_NOTE = ("GPU arm: 256 MiB written before every timed build (L2 flush); "
            "CPU arm: no flush (host caches)")
@@ -59,6 +65,9 @@ def parse():
                     help="held-out molecules of the learned-guess measurement (0 skips it)")
     ap.add_argument("--jk-only", type=int, default=0,
                     help="profiling driver: prepare the workload, run this many J/K builds, print timings, exit")
+    ap.add_argument("--tune-only", type=int, default=0,
+                    help="profiling driver: prepare the workload, run one J/K build and the autotuner "
+                         "(every kernel variant of every class timed this many times), print the choice, exit")
     ap.add_argument("--batched-only", type=int, default=0,
                     help="profiling driver: one batched RHF call over this many molecules of the learned-guess "
                          "test set (3-12 atoms, STO-3G, core-Hamiltonian guess), print timings, exit")
@@ -372,6 +381,16 @@ def run_ours(args):
     value = world * q * args.steps / (total_ms * 1e-3) / 1e9
     e2e_value = world * q * args.steps / e2e_tot / 1e9
     achieved = float(np.mean(flops)) / (total_ms / args.steps * 1e-3) / 1e12
+    # the dominant kernel: every class kernel timed alone (CUDA events on the library's
+    # stream), flops from the generated per-class operation counts
+    class_ms = np.zeros(32, np.float32)
+    ctx.check(lib.qb_jk_class_times(ctx.h, 3, class_ms.ctypes.data_as(C.POINTER(C.c_float))))
+    ftab = json.loads(FLOPS_TABLE.read_text())["classes"]
+    names = ["".join(str(v) for v in stats.class_l[c]) for c in range(stats.nclass)]
+    cflops = [ftab[nm]["prim_flops"] * stats.class_prim_quartets[c] +
+              (ftab[nm]["contr_flops"] + 12 * ftab[nm]["nint"]) * stats.class_quartets[c] for c, nm in enumerate(names)]
+    dom = int(np.argmax(class_ms[:stats.nclass]))
+    dom_achieved = cflops[dom] / (float(class_ms[dom]) * 1e-3) / 1e12
     J = Jp.reshape((n, n), order="F")
     K = Kp.reshape((n, n), order="F")
     sym = float(max(np.abs(J - J.T).max() / np.abs(J).max(), np.abs(K - K.T).max() / np.abs(K).max()))
@@ -388,11 +407,17 @@ def run_ours(args):
                         "autotune_s": t_tune,
                         "kernel_variants": {"".join(str(v) for v in stats.class_l[c]): int(chosen[c])
                                             for c in range(stats.nclass)}},
-            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": None,
+            "roofline": {"bound": "fp64", "achieved": dom_achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": dom_achieved / peak,
+                         "traffic": DOMINANT_TRAFFIC.get(f"{names[dom]}/{int(chosen[dom])}"),
+                         "kernel": f"class ({names[dom][:2]}|{names[dom][2:]}), variant {int(chosen[dom])}",
+                         "kernel_ms": float(class_ms[dom]), "flops_per_launch": float(cflops[dom]),
                          "peak_source": "measured: FP64 FMA microbenchmark (qb_fp64_peak) in this run",
-                         "flops_per_step": float(np.mean(flops)),
-                         "flops_source": "per-class FP64 op counts of the generated kernels x quartets"},
+                         "flops_source": "per-class FP64 op counts of the generated kernels x this launch's "
+                                         "quartets and primitive quartets"},
+            "roofline_build": {"achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                               "flops_per_step": float(np.mean(flops)),
+                               "class_ms_alone": {nm: float(class_ms[c]) for c, nm in enumerate(names)}},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * n * 8,
                     "d2h_bytes_per_step": 2 * n * n * 8, "ms_per_step": 1e3 * e2e_tot / args.steps},
             "gpu_launches": launches_per_step * args.steps,
@@ -659,6 +684,27 @@ def run_jk_only(args):
     print(json.dumps({"class_quartets_prim_quartets": classes}), flush=True)
 
 
+def run_tune_only(args):
+    """One J/K build and one autotuner pass over every kernel variant (for captures of the
+    variants that a build does not run)."""
+    import __graft_entry__ as ge
+    qb = ge.load_package()
+    from quiqbox_gb300 import _lib as L
+    ctx = qb.Context(0)
+    fb, D = workload(qb, args.seed)
+    b = L.BasisArgs(fb)
+    Df = np.ascontiguousarray(D.reshape(-1, order="F"))
+    ctx.check(ctx.lib.qb_jk_prepare(ctx.h, b.ref(), args.schwarz))
+    ctx.check(ctx.lib.qb_jk_upload_density(ctx.h, L.dptr(Df)))
+    st = L.QBJKStats()
+    ctx.check(ctx.lib.qb_jk_execute(ctx.h))
+    ctx.check(ctx.lib.qb_jk_get_stats(ctx.h, C.byref(st)))
+    chosen = np.zeros(32, np.int32)
+    ctx.check(ctx.lib.qb_jk_autotune(ctx.h, args.tune_only, L.iptr(chosen)))
+    print(json.dumps({"".join(str(v) for v in st.class_l[c]): [int(st.class_quartets[c]), int(st.class_prim_quartets[c]),
+                                                                int(chosen[c])] for c in range(st.nclass)}), flush=True)
+
+
 def run_batched_only(args):
     """One batched RHF call (after a small warm-up call) for launch-list captures."""
     import __graft_entry__ as ge
@@ -678,6 +724,9 @@ if __name__ == "__main__":
     a = parse()
     if a.jk_only:
         run_jk_only(a)
+        sys.exit(0)
+    if a.tune_only:
+        run_tune_only(a)
         sys.exit(0)
     if a.batched_only:
         run_batched_only(a)

@@ -78,9 +78,17 @@ int qb_multipole_moments(qb_ctx* ctx, const qb_basis* basis, const double center
  * last qb_jk_prepare and the uploaded density, times every compiled kernel variant of
  * every angular-momentum class on its actual quartet work list (best of `repeats`) and
  * keeps the fastest per class for this context; variants[c] (nclass entries of
- * qb_jk_stats, may be NULL) receives the choice (0: one quartet per thread, 1-3: warp-
- * cooperative configurations).  Costs a few J/K builds; J and K stay those of the density. */
+ * qb_jk_stats, may be NULL) receives the choice (0: one quartet per thread, 1-4: warp-
+ * cooperative configurations, 5: segmented kernel).  Costs a few J/K builds; J and K stay
+ * those of the density. */
 int qb_jk_autotune(qb_ctx* ctx, int repeats, int* variants);
+
+/* Per-class device time of the J/K build (no counterpart in the reference, a measurement
+ * hook): after qb_jk_prepare and a density upload, launches every class kernel alone with
+ * its current variant over its work list on the context stream and times it with CUDA
+ * events, best of `repeats`; ms[c] (nclass entries of qb_jk_stats) receives the time, 0 for
+ * classes without work.  J and K stay those of the density. */
+int qb_jk_class_times(qb_ctx* ctx, int repeats, float* ms);
 
 /* Kernels of the learned initial guess (no counterpart in the reference): a small MLP
  * with BF16 weights and activations and FP32 accumulation, trained and evaluated on the

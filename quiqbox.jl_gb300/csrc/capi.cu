@@ -58,7 +58,7 @@ int qb_create(qb_ctx** out, int device) {
         qb_get_class_launchers(ctx->launch);
         // Variant per class: the generator's measured preference.  QB_JK_VARIANT overrides
         // it for tuning: "thread" (variant 0 everywhere), "warp" (variant 1 wherever
-        // compiled), or one character per class, '0'..'4' (a variant that is not compiled
+        // compiled), or one character per class, '0'..'5' (a variant that is not compiled
         // for a class falls back to the preference).
         const char* ov = getenv("QB_JK_VARIANT");
         for (int c = 0; c < ctx->nclass; ++c) {
@@ -74,6 +74,13 @@ int qb_create(qb_ctx** out, int device) {
             if (!L.jk[v]) v = 0;
             ctx->variant[c] = v;
             ctx->occ[c] = L.occupancy[v]();
+        }
+        // QB_JK_PRIM_EPS overrides the primitive-quartet threshold of the J/K class kernels
+        // (validation of the primitive screening; 0 evaluates every primitive quartet)
+        if (const char* pe = getenv("QB_JK_PRIM_EPS")) {
+            char* end = nullptr;
+            const double v = strtod(pe, &end);
+            if (end != pe && v >= 0.0) ctx->prim_eps = (float)v;
         }
         rc = qb_cuda_check(ctx, cudaGetLastError(), "kernel occupancy query");
     }
@@ -304,6 +311,12 @@ int qb_jk_quartet_list(qb_ctx* ctx, int64_t nq, const int* pairs, double* J, dou
 int qb_jk_autotune(qb_ctx* ctx, int repeats, int* variants) {
     QB_TRY(enter(ctx));
     return qb_jk_autotune_device(ctx, repeats, variants);
+}
+
+int qb_jk_class_times(qb_ctx* ctx, int repeats, float* ms) {
+    QB_TRY(enter(ctx));
+    if (!ms) return qb_set_error(ctx, QB_ERR_ARG, "null output");
+    return qb_jk_class_times_device(ctx, repeats, ms);
 }
 
 int qb_jk_download(qb_ctx* ctx, double* J, double* K) {

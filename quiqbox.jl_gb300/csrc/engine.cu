@@ -265,6 +265,32 @@ __global__ void qb_primpair_compact_kernel(const ShellPair* __restrict__ pairs, 
     nkept[k] = kept;
 }
 
+// Per shell pair: sort its kept primitive pairs by descending screening key (the pad
+// float, here the primitive Schwarz factor) and keep those with key * max key >= eps
+// (negligible against every partner); writes the kept count.
+__global__ void qb_primpair_key_compact_kernel(const ShellPair* __restrict__ pairs, int npair, PrimPair* prims,
+                                               const unsigned* __restrict__ keymax_bits, float eps,
+                                               int* __restrict__ nkept) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= npair) return;
+    const ShellPair sp = pairs[k];
+    const float kmax = __uint_as_float(*keymax_bits);
+    PrimPair* pp = prims + sp.prim0;
+    auto key = [](const PrimPair& x) { return reinterpret_cast<const float*>(&x.pad)[0]; };
+    for (int i = 1; i < sp.nprim; ++i) {
+        const PrimPair x = pp[i];
+        int j = i - 1;
+        while (j >= 0 && key(pp[j]) < key(x)) {
+            pp[j + 1] = pp[j];
+            --j;
+        }
+        pp[j + 1] = x;
+    }
+    int kept = 0;
+    while (kept < sp.nprim && key(pp[kept]) * kmax >= eps) ++kept;
+    nkept[k] = kept;
+}
+
 // FP32 copy (p, P) of every primitive pair, read by the warp-cooperative class kernels
 // to group primitive quartets by Boys-function branch.
 __global__ void qb_primpair_f32_kernel(const PrimPair* __restrict__ prims, int n, float4* __restrict__ out) {
@@ -376,6 +402,39 @@ int qb_ensure_pairs(qb_ctx* ctx) {
         QB_CUDA(ctx, cudaGetLastError());
     }
     QB_TRY(qb_check_status(ctx));
+    // Primitive Schwarz keys: each kept primitive pair's screening key becomes its own
+    // Schwarz factor, the pair's primitives are re-sorted by it and the ones negligible
+    // against every partner dropped; the FP32 centres follow the new order.
+    {
+        DevArray<unsigned> d_keymax;
+        QB_CUDA(ctx, d_keymax.ensure(1));
+        QB_CUDA(ctx, cudaMemsetAsync(d_keymax.p, 0, sizeof(unsigned), s));
+        for (int pc = 0; pc < npc; ++pc) {
+            int la = 0;
+            while ((la + 1) * (la + 2) / 2 <= pc) ++la;
+            const int lb = pc - la * (la + 1) / 2;
+            const int n = ctx->pc_off[pc + 1] - ctx->pc_off[pc];
+            if (n == 0) continue;
+            QbPrimKeyLaunch launch = nullptr;
+            for (int c = 0; c < QB_NCLASS; ++c) {
+                const ClassLaunchers& L = ctx->launch[c];
+                if (L.la == la && L.lb == lb && L.lc == la && L.ld == lb) launch = L.primkey;
+            }
+            if (!launch) return qb_set_error(ctx, QB_ERR_UNSUPPORTED, "no diagonal class for a pair class");
+            launch(ctx->d_pairs.p + ctx->pc_off[pc], n, ctx->d_prims.p, ctx->boys.p, d_keymax.p, s);
+        }
+        if (npair > 0)
+            qb_primpair_key_compact_kernel<<<(npair + 127) / 128, 128, 0, s>>>(ctx->d_pairs.p, npair, ctx->d_prims.p,
+                                                                                d_keymax.p, ctx->prim_eps,
+                                                                                d_nkept.p);
+        if (nslot > 0)
+            qb_primpair_f32_kernel<<<(nslot + 127) / 128, 128, 0, s>>>(ctx->d_prims.p, nslot, ctx->d_prims32.p);
+        QB_CUDA(ctx, cudaGetLastError());
+        std::vector<int> nkept(npair);
+        QB_CUDA(ctx, cudaMemcpyAsync(nkept.data(), d_nkept.p, npair * sizeof(int), cudaMemcpyDeviceToHost, s));
+        QB_CUDA(ctx, cudaStreamSynchronize(s));
+        for (int k = 0; k < npair; ++k) pairs[k].nprim = nkept[k];
+    }
     std::vector<double> Q(npair);
     QB_CUDA(ctx, cudaMemcpyAsync(Q.data(), ctx->d_Q.p, npair * sizeof(double), cudaMemcpyDeviceToHost, s));
     QB_CUDA(ctx, cudaStreamSynchronize(s));
@@ -555,7 +614,7 @@ int qb_jk_device(qb_ctx* ctx, const double* dD, double* dJ, double* dK, double t
         ClassWork w{ctx->d_pairs.p + plan.bra_off[c], ctx->d_pairs.p + plan.ket_off[c],
                     ctx->d_offs.p + plan.offs_off[c], plan.nbra[c], plan.same[c]};
         const int grid = ctx->nsm * std::max(1, ctx->occ[c]);
-        JKArgs args{ctx->d_prims.p, ctx->d_prims32.p, ctx->boys.p, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p, ctx->d_primcount.p + c, n};
+        JKArgs args{ctx->d_prims.p, ctx->d_prims32.p, ctx->boys.p, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p, ctx->d_primcount.p + c, n, ctx->prim_eps};
         ctx->launch[c].jk[ctx->variant[c]](w, args, grid, ctx->streams[k % QB_NSTREAM]);
         ++k;
     }
@@ -613,7 +672,7 @@ int qb_jk_quartets_device(qb_ctx* ctx, long long nq, const int* pq, double* dJ, 
         const int P = pq[2 * q], Q = pq[2 * q + 1], c = cls[q];
         const ClassWork w{ctx->d_pairs.p + P, ctx->d_pairs.p + Q, ctx->d_one_offs.p, 1, P == Q ? 1 : 0};
         const JKArgs args{ctx->d_prims.p, ctx->d_prims32.p, ctx->boys.p, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p,
-                          ctx->d_primcount.p + c, n};
+                          ctx->d_primcount.p + c, n, ctx->prim_eps};
         ctx->launch[c].jk[ctx->variant[c]](w, args, 1, s);
     }
     QB_CUDA(ctx, cudaGetLastError());
@@ -643,7 +702,7 @@ int qb_jk_autotune_device(qb_ctx* ctx, int repeats, int* chosen) {
         const ClassWork w{ctx->d_pairs.p + ctx->pc_off[X], ctx->d_pairs.p + ctx->pc_off[Y],
                           ctx->d_offs.p + ctx->offs_off[c], nbra, X == Y};
         const JKArgs args{ctx->d_prims.p, ctx->d_prims32.p, ctx->boys.p, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p,
-                          ctx->d_primcount.p + c, n};
+                          ctx->d_primcount.p + c, n, ctx->prim_eps};
         float best = 0.f;
         int best_v = ctx->variant[c], best_occ = ctx->occ[c];
         for (int v = 0; v < QB_NVARIANT; ++v) {
@@ -672,6 +731,43 @@ int qb_jk_autotune_device(qb_ctx* ctx, int repeats, int* chosen) {
     }
     QB_CUDA(ctx, cudaGetLastError());
     // the timing runs accumulated into J'/K': leave the context's J and K consistent
+    return qb_jk_device(ctx, ctx->d_D.p, ctx->d_J.p, ctx->d_K.p, ctx->schwarz, s);
+}
+
+// Per-class device time: every class kernel of the current work lists launched alone with
+// its current variant on the context stream (CUDA events, best of `repeats`); then one
+// build, so that J and K stay those of the density.
+int qb_jk_class_times_device(qb_ctx* ctx, int repeats, float* ms) {
+    if (!ctx->jk_prepared) return qb_set_error(ctx, QB_ERR_ARG, "call qb_jk_prepare first");
+    cudaStream_t s = ctx->stream;
+    QB_TRY(qb_jk_device(ctx, ctx->d_D.p, ctx->d_J.p, ctx->d_K.p, ctx->schwarz, s));
+    QB_CUDA(ctx, cudaStreamSynchronize(s));
+    for (int c = 0; c < ctx->nclass; ++c) ms[c] = 0.f;
+    if (!ctx->shell_path) return QB_OK;
+    const int n = ctx->nfun;
+    for (int c = 0; c < ctx->nclass; ++c) {
+        const ClassLaunchers& L = ctx->launch[c];
+        const int X = ctx->class_bra[c], Y = ctx->class_ket[c];
+        const int nbra = ctx->pc_off[X + 1] - ctx->pc_off[X], nket = ctx->pc_off[Y + 1] - ctx->pc_off[Y];
+        if (nbra == 0 || nket == 0) continue;
+        const ClassWork w{ctx->d_pairs.p + ctx->pc_off[X], ctx->d_pairs.p + ctx->pc_off[Y],
+                          ctx->d_offs.p + ctx->offs_off[c], nbra, X == Y};
+        const JKArgs args{ctx->d_prims.p, ctx->d_prims32.p, ctx->boys.p, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p,
+                          ctx->d_primcount.p + c, n, ctx->prim_eps};
+        const int grid = ctx->nsm * std::max(1, ctx->occ[c]);
+        float best = 0.f;
+        for (int r = 0; r < std::max(1, repeats); ++r) {
+            QB_CUDA(ctx, cudaEventRecord(ctx->ev_start, s));
+            L.jk[ctx->variant[c]](w, args, grid, s);
+            QB_CUDA(ctx, cudaEventRecord(ctx->ev_stop, s));
+            QB_CUDA(ctx, cudaEventSynchronize(ctx->ev_stop));
+            float t = 0.f;
+            QB_CUDA(ctx, cudaEventElapsedTime(&t, ctx->ev_start, ctx->ev_stop));
+            best = (r == 0) ? t : std::min(best, t);
+        }
+        ms[c] = best;
+    }
+    QB_CUDA(ctx, cudaGetLastError());
     return qb_jk_device(ctx, ctx->d_D.p, ctx->d_J.p, ctx->d_K.p, ctx->schwarz, s);
 }
 

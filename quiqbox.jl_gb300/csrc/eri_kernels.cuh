@@ -26,6 +26,7 @@ struct JKArgs {
     double* Kp;                            // K' accumulator
     unsigned long long* primcount;         // primitive quartets evaluated (this class)
     int nfun;
+    float prim_eps;                        // primitive-quartet threshold on the screening-key product
 };
 
 __device__ __forceinline__ int qb_find_bra(const long long* __restrict__ offs, int n, long long t) {
@@ -152,7 +153,7 @@ __global__ void __launch_bounds__(128) qb_jk_class_kernel(const ClassWork w, con
         const ShellPair Q = w.ket[j];
         double I[C::NINT];
         C::block(a.prims + P.prim0, P.nprim, a.prims + Q.prim0, Q.nprim, P.ABx, P.ABy, P.ABz, Q.ABx, Q.ABy, Q.ABz,
-                 a.boys, I, nprimq);
+                 a.boys, I, nprimq, a.prim_eps);
         const double deg = (P.same ? 1.0 : 2.0) * (Q.same ? 1.0 : 2.0) * ((w.same && i == j) ? 1.0 : 2.0);
         qb_jk_digest<C>(P, Q, deg, a, I);
     }
@@ -295,7 +296,7 @@ __global__ void __launch_bounds__(32 * WPB) qb_jk_warp_kernel(const ClassWork w,
     double* acc = qb_dyn_smem + (size_t)warp * PER_WARP;
     const long long total = __ldg(w.offs + w.nbra);
     const long long stride = (long long)gridDim.x * WPB * G;
-    const float eps = (float)QB_PRIM_EPS;
+    const float eps = a.prim_eps;
     unsigned long long nprim_warp = 0;
 
     // the owner's q-th significant primitive quartet -> (bra, ket) primitive-pair indices
@@ -500,18 +501,197 @@ __global__ void __launch_bounds__(32 * WPB) qb_jk_warp_kernel(const ClassWork w,
     if (lane == 0 && nprim_warp) atomicAdd(a.primcount, nprim_warp);
 }
 
+// Reduce-scatter of eight values over the eight lanes of an aligned lane segment (j8 =
+// lane & 7): lane j8 ends with the segment's sum of its value j8 and adds it to row[j8].
+// Three exchange stages (lane ^ 4, ^ 2, ^ 1), each halving the values a lane holds: seven
+// FP64 adds and fourteen 32-bit shuffles per eight values, no atomics.  Every lane of the
+// warp calls it.
+__device__ __forceinline__ void qb_rs8_add(double* row, int j8, double v0, double v1, double v2, double v3,
+                                           double v4, double v5, double v6, double v7) {
+    const unsigned FULL = 0xffffffffu;
+    const bool h2 = j8 & 4, h1 = j8 & 2, h0 = j8 & 1;
+    const double a0 = (h2 ? v4 : v0) + __shfl_xor_sync(FULL, h2 ? v0 : v4, 4);
+    const double a1 = (h2 ? v5 : v1) + __shfl_xor_sync(FULL, h2 ? v1 : v5, 4);
+    const double a2 = (h2 ? v6 : v2) + __shfl_xor_sync(FULL, h2 ? v2 : v6, 4);
+    const double a3 = (h2 ? v7 : v3) + __shfl_xor_sync(FULL, h2 ? v3 : v7, 4);
+    const double b0 = (h1 ? a2 : a0) + __shfl_xor_sync(FULL, h1 ? a0 : a2, 2);
+    const double b1 = (h1 ? a3 : a1) + __shfl_xor_sync(FULL, h1 ? a1 : a3, 2);
+    const double c = (h0 ? b1 : b0) + __shfl_xor_sync(FULL, h0 ? b0 : b1, 1);
+    row[j8] += c;
+}
+
+#define QB_SEG_MAXNB 16   // bra primitive pairs whose ket counts the segmented kernel tabulates
+
+// Segmented kernel (classes with many contracted targets).  A warp takes a batch of G <= 32
+// contracted quartets ("owners"; G from the class's quartets per warp, at least four
+// batches per warp), sorts them by their number of significant primitive quartets and
+// runs them four at a time, one per 8-lane segment: in each round a segment's lanes
+// evaluate eight of its owner's primitive quartets (lanes past the owner's count run a
+// valid primitive quartet with a zero prefactor), and every group of eight VRR targets is
+// reduce-scattered over the segment (qb_rs8_add) into the owner's shared-memory row, one
+// plain add per lane and target: no atomics, so no compare-and-swap retries when many
+// lanes serve one quartet, and no accumulator in registers or local memory.  Sorting makes
+// the four owners of a wave need similar round counts.  After a wave the whole warp runs
+// each owner's HRR and J/K digestion from shared memory (as the cooperative epilogue of
+// qb_jk_warp_kernel).
+template <class C>
+struct QbSeg {
+    static constexpr int NR = C::NSEGB * 8;   // row length: emission slots of the targets
+    static constexpr int NI = C::NINT > C::NT ? C::NINT : C::NT;
+    static constexpr int doubles = 4 * NR + C::NA * C::NB * C::NF + NI;   // per warp
+};
+
+template <int LA, int LB, int LC, int LD, int WPB>
+__global__ void __launch_bounds__(32 * WPB) qb_jk_seg_kernel(const ClassWork w, const JKArgs a) {
+    using C = EriClass<LA, LB, LC, LD>;
+    constexpr int GMAX = 32;
+    constexpr int NR = QbSeg<C>::NR;
+    constexpr int NAB = C::NA * C::NB, NCD = C::NC * C::ND, NF = C::NF, NT = C::NT;
+    extern __shared__ double qb_dyn_smem[];
+    __shared__ unsigned short s_cnt[WPB][GMAX][QB_SEG_MAXNB];
+    __shared__ int s_prim0b[WPB][GMAX], s_prim0k[WPB][GMAX], s_nb[WPB][GMAX], s_nk[WPB][GMAX], s_tot[WPB][GMAX];
+    __shared__ unsigned char s_order[WPB][GMAX];
+    const unsigned FULL = 0xffffffffu;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, seg = lane >> 3, j8 = lane & 7;
+    double* rows = qb_dyn_smem + (size_t)warp * QbSeg<C>::doubles;
+    double* Tb = rows + 4 * NR;    // (ab|f) of the current owner, [ab][f]
+    double* Ib = Tb + NAB * NF;    // the owner's targets in (e, f) order, then its (ab|cd) block
+    const long long total = __ldg(w.offs + w.nbra);
+    const long long nwarps = (long long)gridDim.x * WPB;
+    // owners per batch: a multiple of 4 in [4, 32], about a sixth of the quartets per warp
+    const int G = (int)max(4LL, min((long long)GMAX, (total / nwarps / 6) & ~3LL));
+    const long long stride = nwarps * G;
+    const float eps = a.prim_eps;
+    unsigned long long nprim = 0;
+
+    auto decode = [&](int owner, int q, int& bpi, int& kpi) {
+        int ib = 0, rem = q;
+        if (s_nb[warp][owner] <= QB_SEG_MAXNB) {
+            while (rem >= s_cnt[warp][owner][ib]) { rem -= s_cnt[warp][owner][ib]; ++ib; }
+        } else {
+            const PrimPair* bp = a.prims + s_prim0b[warp][owner];
+            const PrimPair* kp = a.prims + s_prim0k[warp][owner];
+            const int nk = s_nk[warp][owner];
+            for (;;) {
+                const float kb = qb_kabs(bp + ib);
+                int n = 1;
+                while (n < nk && kb * qb_kabs(kp + n) >= eps) ++n;
+                if (rem < n) break;
+                rem -= n;
+                ++ib;
+            }
+        }
+        bpi = s_prim0b[warp][owner] + ib;
+        kpi = s_prim0k[warp][owner] + rem;
+    };
+
+    for (long long base = ((long long)blockIdx.x * WPB + warp) * G; base < total; base += stride) {
+        const long long t = base + lane;
+        const bool valid = lane < G && t < total;
+        int i = 0, j = 0, mytot = 0;
+        if (valid) {
+            i = qb_find_bra(w.offs, w.nbra, t);
+            j = (int)(t - __ldg(w.offs + i));
+            const ShellPair P = w.bra[i];
+            const ShellPair Q = w.ket[j];
+            const PrimPair* bp = a.prims + P.prim0;
+            const PrimPair* kp = a.prims + Q.prim0;
+            if (Q.nprim > 0) {
+                const float kmax_ket = qb_kabs(kp);
+                for (int ib = 0; ib < P.nprim; ++ib) {
+                    const float kb = qb_kabs(bp + ib);
+                    if (kb * kmax_ket < eps) break;
+                    int n = 1;
+                    while (n < Q.nprim && kb * qb_kabs(kp + n) >= eps) ++n;
+                    if (ib < QB_SEG_MAXNB) s_cnt[warp][lane][ib] = (unsigned short)n;
+                    mytot += n;
+                }
+            }
+            s_prim0b[warp][lane] = P.prim0;
+            s_prim0k[warp][lane] = Q.prim0;
+            s_nb[warp][lane] = P.nprim;
+            s_nk[warp][lane] = Q.nprim;
+        }
+        // valid owners (a prefix of the lanes) ranked by descending count, ties by lane:
+        // positions 0..nown-1 of s_order are the valid owners
+        int rank = 0;
+        for (int m = 0; m < G; ++m) {
+            const int tm = __shfl_sync(FULL, mytot, m);
+            rank += (tm > mytot) || (tm == mytot && m < lane);
+        }
+        if (lane < G) {
+            s_order[warp][rank] = (unsigned char)lane;
+            s_tot[warp][rank] = mytot;
+        }
+        const int nown = __popc(__ballot_sync(FULL, valid));
+        __syncwarp();
+        for (int w0 = 0; w0 < nown; w0 += 4) {
+            const int o = w0 + seg;
+            const bool has = o < nown;
+            const int ow = s_order[warp][has ? o : w0];
+            const int tot = has ? s_tot[warp][o] : 0;
+            const int rounds = (s_tot[warp][w0] + 7) >> 3;   // the wave's largest count
+            for (int e = lane; e < 4 * NR; e += 32) rows[e] = 0.0;
+            __syncwarp();
+            double* row = rows + seg * NR;
+            for (int r = 0; r < rounds; ++r) {
+                const int q = r * 8 + j8;
+                const bool act = q < tot;
+                int bpi = s_prim0b[warp][ow], kpi = s_prim0k[warp][ow];
+                if (act) decode(ow, q, bpi, kpi);
+                PrimPair B = qb_load_pair(a.prims + bpi);
+                const PrimPair Kt = qb_load_pair(a.prims + kpi);
+                if (!act) B.K = 0.0;   // zero prefactor: every target of this lane is zero
+                C::prim_seg(B, Kt, a.boys,
+                            [&](int b, double v0, double v1, double v2, double v3, double v4, double v5, double v6,
+                                double v7) { qb_rs8_add(row + 8 * b, j8, v0, v1, v2, v3, v4, v5, v6, v7); });
+            }
+            if (j8 == 0) nprim += tot;
+            __syncwarp();
+            const int nw = min(4, nown - w0);
+            for (int g = 0; g < nw; ++g) {
+                const int og = s_order[warp][w0 + g];
+                const int ig = __shfl_sync(FULL, i, og), jg = __shfl_sync(FULL, j, og);
+                const ShellPair Pg = w.bra[ig];
+                const ShellPair Qg = w.ket[jg];
+                const unsigned short* pos = C::seg_pos();
+                const double* rg = rows + g * NR;
+                for (int k = lane; k < NT; k += 32) Ib[k] = rg[pos[k]];
+                __syncwarp();
+                for (int f = lane; f < NF; f += 32)
+                    C::hrr_bra(QbColumnSum<1>{Ib + f, NF, 0}, Pg.ABx, Pg.ABy, Pg.ABz,
+                               [&](int ab, double v) { Tb[ab * NF + f] = v; });
+                __syncwarp();
+                for (int ab = lane; ab < NAB; ab += 32)
+                    C::hrr_ket(Tb + ab * NF, Qg.ABx, Qg.ABy, Qg.ABz, [&](int cd, double v) { Ib[ab * NCD + cd] = v; });
+                __syncwarp();
+                const double deg = (Pg.same ? 1.0 : 2.0) * (Qg.same ? 1.0 : 2.0) * ((w.same && ig == jg) ? 1.0 : 2.0);
+                qb_jk_digest_warp<C>(Pg, Qg, deg, a, Ib, lane);
+                __syncwarp();
+            }
+        }
+        __syncwarp();
+    }
+    for (int d = 16; d > 0; d >>= 1) nprim += __shfl_down_sync(FULL, nprim, d);
+    if (lane == 0 && nprim) atomicAdd(a.primcount, nprim);
+}
+
 // Host-side launchers, one set per class (defined in the generated eri_class_*.cu).
-// Variant 0 runs one contracted quartet per thread (qb_jk_class_kernel); variants 1..3
-// are configurations of the warp-cooperative kernel (null where not compiled).
-#define QB_NVARIANT 5
+// Variant 0 runs one contracted quartet per thread (qb_jk_class_kernel); variants 1..4
+// are configurations of the warp-cooperative kernel, variant 5 the segmented kernel (null
+// where not compiled).
+#define QB_NVARIANT 6
 typedef void (*QbSchwarzLaunch)(const ShellPair* pairs, int n, const PrimPair* prims, const double* boys,
                                 const double* ratio, double* Q, cudaStream_t s);
+typedef void (*QbPrimKeyLaunch)(const ShellPair* pairs, int n, PrimPair* prims, const double* boys, unsigned* keymax,
+                                cudaStream_t s);
 struct ClassLaunchers {
     void (*jk[QB_NVARIANT])(const ClassWork&, const JKArgs&, int grid, cudaStream_t);
     int (*occupancy[QB_NVARIANT])(void);   // resident blocks per SM (also sets the shared-memory limit)
     int la, lb, lc, ld;
     int preferred;                         // default variant
     QbSchwarzLaunch schwarz;               // diagonal classes (ab|ab): Schwarz factors of pair class (a, b)
+    QbPrimKeyLaunch primkey;               // diagonal classes: primitive Schwarz keys of pair class (a, b)
 };
 
 // Schwarz factors Q_ab = max over components sqrt|(ab|ab)| of one pair class from the
@@ -542,11 +722,43 @@ __global__ void __launch_bounds__(128) qb_schwarz_class_kernel(const ShellPair* 
     Q[k] = sqrt(mx);
 }
 
+// Primitive Schwarz factors of one pair class: for every kept primitive pair (ab) of every
+// shell pair, key = sqrt(max over components |(ab|ab)|) of the ratio-free shells (the
+// class's own quartet code on the one primitive quartet (ab|ab)), stored as the pair's
+// FP32 screening key; keymax receives the largest key (positive floats order as their bits).
+template <int LA, int LB>
+__global__ void __launch_bounds__(128) qb_prim_key_kernel(const ShellPair* __restrict__ pairs, int n,
+                                                          PrimPair* prims, const double* __restrict__ boys,
+                                                          unsigned* keymax) {
+    using C = EriClass<LA, LB, LA, LB>;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const ShellPair P = pairs[k];
+    float kmax = 0.f;
+    for (int u = 0; u < P.nprim; ++u) {
+        PrimPair* pp = prims + P.prim0 + u;
+        double I[C::NINT];
+        unsigned cnt = 0;
+        C::block(pp, 1, pp, 1, P.ABx, P.ABy, P.ABz, P.ABx, P.ABy, P.ABz, boys, I, cnt, 0.f);
+        double mx = 0.0;
+        for (int x = 0; x < C::NA; ++x)
+            for (int y = 0; y < C::NB; ++y) mx = fmax(mx, fabs(I[((x * C::NB + y) * C::NA + x) * C::NB + y]));
+        const float key = (float)sqrt(mx);
+        reinterpret_cast<float*>(&pp->pad)[0] = key;
+        kmax = fmaxf(kmax, key);
+    }
+    atomicMax(keymax, __float_as_uint(kmax));
+}
+
 #define QB_DEFINE_SCHWARZ_LAUNCHER(LA, LB)                                                                     \
     static void qb_schwarz_launch_##LA##LB##LA##LB(const ShellPair* p, int n, const PrimPair* prims,           \
                                                    const double* boys, const double* ratio, double* Q,         \
                                                    cudaStream_t s) {                                           \
         if (n > 0) qb_schwarz_class_kernel<LA, LB><<<(n + 127) / 128, 128, 0, s>>>(p, n, prims, boys, ratio, Q); \
+    }                                                                                                          \
+    static void qb_primkey_launch_##LA##LB##LA##LB(const ShellPair* p, int n, PrimPair* prims,                 \
+                                                   const double* boys, unsigned* keymax, cudaStream_t s) {     \
+        if (n > 0) qb_prim_key_kernel<LA, LB><<<(n + 127) / 128, 128, 0, s>>>(p, n, prims, boys, keymax);     \
     }
 
 #define QB_DEFINE_LAUNCHERS(LA, LB, LC, LD)                                                                  \
@@ -578,5 +790,22 @@ __global__ void __launch_bounds__(128) qb_schwarz_class_kernel(const ShellPair* 
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb,                                                   \
                                                       qb_jk_warp_kernel<LA, LB, LC, LD, WPB, G, S, RG, PL, CO>, \
                                                       32 * (WPB), QB_WARP_SMEM(LA, LB, LC, LD, WPB, G, S, CO)); \
+        return nb;                                                                                           \
+    }
+
+#define QB_SEG_SMEM(LA, LB, LC, LD, WPB) ((size_t)(WPB) * QbSeg<EriClass<LA, LB, LC, LD>>::doubles * sizeof(double))
+
+// Segmented-kernel configuration V of class LA LB LC LD (WPB warps per block).
+#define QB_DEFINE_SEG_LAUNCHERS(V, LA, LB, LC, LD, WPB)                                                      \
+    static void qb_jkw##V##_launch_##LA##LB##LC##LD(const ClassWork& w, const JKArgs& a, int grid,          \
+                                                    cudaStream_t s) {                                        \
+        qb_jk_seg_kernel<LA, LB, LC, LD, WPB><<<grid, 32 * (WPB), QB_SEG_SMEM(LA, LB, LC, LD, WPB), s>>>(w, a); \
+    }                                                                                                        \
+    static int qb_occw##V##_##LA##LB##LC##LD(void) {                                                         \
+        cudaFuncSetAttribute(qb_jk_seg_kernel<LA, LB, LC, LD, WPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             (int)QB_SEG_SMEM(LA, LB, LC, LD, WPB));                                         \
+        int nb = 0;                                                                                          \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, qb_jk_seg_kernel<LA, LB, LC, LD, WPB>, 32 * (WPB),   \
+                                                      QB_SEG_SMEM(LA, LB, LC, LD, WPB));                     \
         return nb;                                                                                           \
     }

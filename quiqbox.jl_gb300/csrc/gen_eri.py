@@ -97,6 +97,7 @@ class ClassGen:
         self.contr = Counter()    # per contracted quartet (HRR)
         self.esets = [e for L in range(la, la + lb + 1) for e in comps(L)]
         self.fsets = [f for L in range(lc, lc + ld + 1) for f in comps(L)]
+        self.seg = len(self.esets) * len(self.fsets) >= SEG_MIN_NT
 
     # -- VRR dependency analysis ------------------------------------------------
     def vrr_children(self, node):
@@ -169,10 +170,28 @@ class ClassGen:
             return f"F{m}"
         return f"v{tname(e)}_{tname(f)}_{m}"
 
-    def emit_vrr(self, out, ind):
+    def emit_vrr(self, out, ind, seg=False):
+        """The VRR body.  seg=False: sink(k, value) per target as soon as it is final.
+        seg=True: targets are gathered in emission order into batches of SEG_W values and
+        each full batch goes to red(b, v0, ..., v7) (the last one padded with zeros);
+        self.seg_pos[k] is then the emission slot of target k."""
         order, targets = self.vrr_nodes()
         tindex = {t: k for k, t in enumerate(targets)}
-        c = self.prim
+        c = self.prim if not seg else Counter()
+        pending = []
+        self.seg_pos = [None] * len(targets)
+        nbatch = [0]
+
+        def emit_target(k, name):
+            if not seg:
+                out.append(f"{ind}sink({k}, {name});")
+                return
+            self.seg_pos[k] = nbatch[0] * SEG_W + len(pending)
+            pending.append(name)
+            if len(pending) == SEG_W:
+                out.append(f"{ind}red({nbatch[0]}, {', '.join(pending)});")
+                pending.clear()
+                nbatch[0] += 1
         for n in order:
             e, f, m = n
             if sum(e) == 0 and sum(f) == 0:
@@ -210,10 +229,14 @@ class ClassGen:
                     c.fma += 2
             out.append(f"{ind}const double {nm} = {expr};")
             if n in tindex:
-                out.append(f"{ind}sink({tindex[n]}, {nm});")
+                emit_target(tindex[n], nm)
         for k, t in enumerate(targets):
             if sum(t[0]) == 0 and sum(t[1]) == 0:
-                out.append(f"{ind}sink({k}, {self.vname(t)});")
+                emit_target(k, self.vname(t))
+        if seg and pending:
+            out.append(f"{ind}red({nbatch[0]}, {', '.join(pending + ['0.0'] * (SEG_W - len(pending)))});")
+            nbatch[0] += 1
+        self.seg_nbatch = nbatch[0]
         c.add += len(targets)   # the accumulation of every target into its contracted sum
         used_m = sorted({n[2] for n in order if sum(n[0]) == 0 and sum(n[1]) == 0})
         maxo2p = max([n[0][pick_axis(n[0])] - 1 for n in order if sum(n[1]) == 0 and sum(n[0]) > 0] + [0])
@@ -412,6 +435,25 @@ class ClassGen:
         o += setup
         o += body
         o.append("  }")
+        if self.seg:
+            prim_head = o[o.index("  template <class Sink>") + 3: o.index(setup[0])]
+            seg_body = []
+            self.emit_vrr(seg_body, ind, seg=True)
+            o.append(f"  // The same VRR for the segmented kernel: targets in emission order, {SEG_W} at a time,")
+            o.append(f"  // go to red(batch, v0..v{SEG_W - 1}) ({self.seg_nbatch} batches; the slot of target k is")
+            o.append("  // seg_pos()[k]).")
+            o.append(f"  static constexpr int NSEGB = {self.seg_nbatch};")
+            o.append(f"  static __device__ __forceinline__ const unsigned short* seg_pos() {{ return qb_seg_pos_{self.name}; }}")
+            o.append("  template <class Red>")
+            o.append("  static __device__ __forceinline__ void prim_seg(const PrimPair& B, const PrimPair& Kt,")
+            o.append("                                                  const double* __restrict__ boys_tab, Red&& red) {")
+            o += prim_head
+            o += setup
+            o += seg_body
+            o.append("  }")
+            table = (f"static __device__ const unsigned short qb_seg_pos_{self.name}[{len(self.seg_pos)}] = {{" +
+                     ", ".join(str(v) for v in self.seg_pos) + "};")
+            o.insert(o.index(f"template <> struct EriClass<{la}, {lb}, {lc}, {ld}> {{"), table)
         o.append("  // Contracted targets -> (ab|cd) block by the horizontal recursion.")
         o.append("  // A[k] is the contracted target k: a register array or a shared-memory row.")
         o.append("  template <class Acc>")
@@ -427,19 +469,21 @@ class ClassGen:
         o.append("  // The same HRR as two one-dimensional transforms (warp-cooperative epilogue).")
         self.emit_hrr_split(o)
         o.append("  // One contracted quartet in one thread: a flattened loop over the primitive quartets")
-        o.append("  // with |K_ab K_cd| >= eps (pairs sorted by descending |K|; eps = 0 evaluates all of")
-        o.append("  // them, as the Schwarz factors need), then the HRR.")
+        o.append("  // whose screening keys (qb_kabs: |K|, or the primitive Schwarz factor; pairs sorted by")
+        o.append("  // descending key) multiply to >= eps (eps = 0 evaluates all of them, as the Schwarz")
+        o.append("  // factors need), then the HRR.")
         o.append("  static __device__ __forceinline__ void block(")
         o.append("      const PrimPair* __restrict__ bp, int nbp, const PrimPair* __restrict__ kp, int nkp,")
         o.append("      double ABx, double ABy, double ABz, double CDx, double CDy, double CDz,")
         o.append("      const double* __restrict__ boys_tab, double (&I)[NINT], unsigned& nprimq,")
-        o.append("      const double eps = QB_PRIM_EPS) {")
+        o.append("      const float eps = (float)QB_PRIM_EPS) {")
         o.append("    double A[NT];")
         o.append("#pragma unroll")
         o.append("    for (int t = 0; t < NT; ++t) A[t] = 0.0;")
-        o.append("    const double kmax_ket = nkp > 0 ? fabs(__ldg(&kp[0].K)) : 0.0;")
+        o.append("    const float kmax_ket = nkp > 0 ? qb_kabs(kp) : 0.f;")
         o.append("    int ib = 0, ik = 0;")
-        o.append("    bool active = nbp > 0 && fabs(__ldg(&bp[0].K)) * kmax_ket >= eps;")
+        o.append("    float kb = nbp > 0 ? qb_kabs(bp) : 0.f;")
+        o.append("    bool active = nbp > 0 && nkp > 0 && kb * kmax_ket >= eps;")
         o.append("    PrimPair B;")
         o.append("    if (active) B = qb_load_pair(bp);")
         o.append("    while (active) {")
@@ -447,11 +491,16 @@ class ClassGen:
         o.append("      ++nprimq;")
         o.append("      prim(B, Kt, boys_tab, [&](int t, double v) { A[t] += v; });")
         o.append("      ++ik;")
-        o.append("      if (ik >= nkp || fabs(B.K * __ldg(&kp[ik].K)) < eps) {")
+        o.append("      if (ik >= nkp || kb * qb_kabs(kp + ik) < eps) {")
         o.append("        ++ib;")
         o.append("        ik = 0;")
-        o.append("        if (ib >= nbp || fabs(__ldg(&bp[ib].K)) * kmax_ket < eps) active = false;")
-        o.append("        else B = qb_load_pair(bp + ib);")
+        o.append("        if (ib >= nbp) {")
+        o.append("          active = false;")
+        o.append("        } else {")
+        o.append("          kb = qb_kabs(bp + ib);")
+        o.append("          if (kb * kmax_ket < eps) active = false;")
+        o.append("          else B = qb_load_pair(bp + ib);")
+        o.append("        }")
         o.append("      }")
         o.append("    }")
         o.append("    hrr(A, ABx, ABy, ABz, CDx, CDy, CDz, I);")
@@ -472,9 +521,27 @@ SMEM_PER_WARP = 50 * 1024
 
 # Default variant per class (0: per-thread kernel), measured on GB300 with the J/K build
 # of 64 H + 16 C/N/O, 3-primitive s/p/d shells.  Classes not listed use variant 1.
-PREFERRED = {"2211": 0, "2221": 0, "2111": 4, "2121": 4, "2220": 4, "2222": 4,
+PREFERRED = {"2211": 5, "2221": 5, "2111": 5, "2121": 5, "2220": 4, "2222": 4,
              "0000": 2, "1000": 2, "1010": 2, "1100": 2, "2000": 2, "2010": 2, "2100": 2,
              "1110": 3, "2020": 3}
+
+
+# Segmented kernel (variant 5, classes with >= SEG_MIN_NT contracted targets): four lane
+# segments of SEG_W lanes per warp, one contracted quartet per segment; the segment's
+# lanes evaluate SEG_W of its primitive quartets at a time and reduce-scatter the targets
+# over the segment (shuffles, no atomics) into the quartet's shared-memory row.
+SEG_W = 8
+SEG_MIN_NT = 90
+SEG_STATIC_PER_WARP = 2560     # bytes of static shared memory per warp (tables) in qb_jk_seg_kernel
+SMEM_LIMIT = 227 * 1024
+
+
+def seg_warps(nsegb, nab, nf, nint, nt):
+    """Warps per block of the segmented kernel: as many as shared memory allows, at most 8,
+    and 4 for the classes of >= 400 targets (at 8 warps ptxas gives their VRR 32 registers
+    and keeps everything else in local memory; at 4 it uses 255)."""
+    per_warp = 8 * (4 * nsegb * SEG_W + nab * nf + max(nint, nt)) + SEG_STATIC_PER_WARP
+    return max(1, min(8 if nt < 400 else 4, SMEM_LIMIT // per_warp))
 
 
 COOP_MIN_NINT = 324   # classes with at least this many integrals get the cooperative epilogue
@@ -535,8 +602,14 @@ def main(outdir, lmax=LMAX_DEFAULT):
               f'#include "eri_class_{name}.cuh"', '#include "eri_kernels.cuh"',
               f'QB_DEFINE_LAUNCHERS({la}, {lb}, {lc}, {ld})']
         jk, occ = [f"qb_jk_launch_{name}"], [f"qb_occ_{name}"]
-        for v in (1, 2, 3, 4):
-            if v in cfgs:
+        if g.seg:
+            cfgs[5] = seg_warps(g.seg_nbatch, ncart(la) * ncart(lb), len(g.fsets), nint_c, nt)
+        for v in (1, 2, 3, 4, 5):
+            if v == 5 and v in cfgs:
+                cu.append(f"QB_DEFINE_SEG_LAUNCHERS({v}, {la}, {lb}, {lc}, {ld}, {cfgs[5]})")
+                jk.append(f"qb_jkw{v}_launch_{name}")
+                occ.append(f"qb_occw{v}_{name}")
+            elif v in cfgs:
                 G_, S_, rg, pl, co, wpb = cfgs[v]
                 cu.append(f"QB_DEFINE_WARP_LAUNCHERS({v}, {la}, {lb}, {lc}, {ld}, {wpb}, {G_}, {S_}, "
                           f"{'true' if rg else 'false'}, {'true' if pl else 'false'}, "
@@ -547,12 +620,12 @@ def main(outdir, lmax=LMAX_DEFAULT):
                 jk.append("nullptr")
                 occ.append("nullptr")
         pref = PREFERRED.get(name, 1 if 1 in cfgs else 0)
-        schwarz = "nullptr"
+        schwarz, primkey = "nullptr", "nullptr"
         if (la, lb) == (lc, ld):
             cu.append(f"QB_DEFINE_SCHWARZ_LAUNCHER({la}, {lb})")
-            schwarz = f"qb_schwarz_launch_{name}"
+            schwarz, primkey = f"qb_schwarz_launch_{name}", f"qb_primkey_launch_{name}"
         cu.append(f"ClassLaunchers qb_class_{name}() {{ return {{{{{', '.join(jk)}}}, {{{', '.join(occ)}}}, "
-                  f"{la}, {lb}, {lc}, {ld}, {pref}, {schwarz}}}; }}")
+                  f"{la}, {lb}, {lc}, {ld}, {pref}, {schwarz}, {primkey}}}; }}")
         (outdir / f"eri_class_{name}.cu").write_text("\n".join(cu) + "\n")
         files.append(name)
         table[name] = {"prim_flops": g.prim.flops(), "contr_flops": g.contr.flops(),

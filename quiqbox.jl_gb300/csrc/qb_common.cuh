@@ -26,9 +26,17 @@
 #define QB_BOYS_TABLE_SIZE (QB_BOYS_EXP_OFF + QB_BOYS_NROW)
 #define QB_BOYS_ASYM_NOEXP_M 6
 
-// Primitive quartets with |K_ab K_cd| below this bound are skipped by the class
-// kernels (the prefactor of every integral of the quartet is below 2.3 x this).
+// Primitive quartets with |K_ab K_cd| below this bound are skipped by the batched
+// integral stores (the prefactor of every integral of the quartet is below 2.3 x this).
 #define QB_PRIM_EPS 1e-20
+
+// Primitive quartets whose primitive Schwarz factors multiply to less than this are
+// skipped by the single-basis J/K kernels.  The key of a primitive pair (ab) is
+// sqrt(max over components |(ab|ab)|) of the ratio-free shells, so by the Cauchy-Schwarz
+// inequality every integral of a skipped primitive quartet is below this bound; with the
+// per-function ratios (<= 3 per d pair) and at most 81 primitive quartets per quartet of
+// 3-primitive shells, a contracted integral changes by < 7.3e-13.
+#define QB_PRIM_EPS_Q 1e-15
 
 // Largest total angular momentum of the generic (per-function) kernels.
 #define QB_GEN_LTOT_MAX 32
@@ -157,8 +165,9 @@ __device__ __forceinline__ PrimPair qb_load_pair(const PrimPair* __restrict__ pt
     return r;
 }
 
-// |K| of a primitive pair as a float, kept in the pad word (screening decisions in
-// the FP32 pipe).
+// Screening key of a primitive pair as a float, kept in the pad word (screening decisions
+// in the FP32 pipe): |K| as built, replaced by the primitive Schwarz factor in the
+// single-basis J/K engine (qb_prim_key_kernel).
 __device__ __forceinline__ float qb_kabs(const PrimPair* __restrict__ p) {
     return __ldg(reinterpret_cast<const float*>(&p->pad));
 }

@@ -83,6 +83,7 @@ int qb_build_prim_pairs(cudaStream_t s, const PairSlot* d_slots, int nslot, cons
                         PrimPair* d_prims, float4* d_prims32, int* d_nkept, unsigned long long* d_kmax);
 
 int qb_jk_autotune_device(qb_ctx* ctx, int repeats, int* chosen);
+int qb_jk_class_times_device(qb_ctx* ctx, int repeats, float* ms);
 int qb_jk_quartets_device(qb_ctx* ctx, long long nq, const int* pq, double* dJ, double* dK);
 int qb_lowest_eig(cudaStream_t s, int n, int k, double* A, double* Y, double* w, double* work);
 int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nnuc, const double* Z,
@@ -132,6 +133,7 @@ struct qb_ctx {
     int nclass = 0;
     int occ[QB_MAX_CLASS] = {};
     int variant[QB_MAX_CLASS] = {};   // launcher variant per class (0 per-thread, 1 warp-cooperative)
+    float prim_eps = (float)QB_PRIM_EPS_Q;   // primitive-quartet threshold of the J/K class kernels
     int class_bra[QB_MAX_CLASS] = {}, class_ket[QB_MAX_CLASS] = {};
     long long offs_off[QB_MAX_CLASS + 1] = {};
     DevArray<long long> d_offs;

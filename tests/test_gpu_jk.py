@@ -138,12 +138,13 @@ np.savez(sys.argv[1], **out)
 """
 
 
-@pytest.mark.parametrize("variant", ["thread", "warp", "2" * 21, "3" * 21, "4" * 21])
+@pytest.mark.parametrize("variant", ["thread", "warp", "2" * 21, "3" * 21, "4" * 21, "5" * 21])
 def test_jk_kernel_variants(qb, oracle, tmp_path, variant):
     # Every class-kernel variant (one contracted quartet per thread; the configurations of
     # the warp-cooperative kernel with pooled primitive quartets; "4": its cooperative
-    # HRR/digestion epilogue, compiled for the classes of >= 81 integrals), selected per
-    # process through QB_JK_VARIANT.  "long" has
+    # HRR/digestion epilogue, compiled for the classes of >= 81 integrals; "5": the segmented
+    # kernel with reduce-scattered accumulation, compiled for the classes of >= 90 targets),
+    # selected per process through QB_JK_VARIANT.  "long" has
     # 6-primitive shells: 36 primitive pairs per shell pair and up to 1296 primitive
     # quartets per contracted quartet, beyond the warp kernel's tabulated counts (32) and
     # its per-pass level window (256).
@@ -173,7 +174,7 @@ def test_jk_autotune_keeps_results(qb, oracle):
     fb, D = _small_shell_system(qb, 0, n_h=2, n_heavy=1, box=4.0)
     ctx = qb.Context(0)
     chosen = qb.jk_autotune(fb, D, schwarz=0.0, ctx=ctx)
-    assert len(chosen) == 21 and all(0 <= v <= 4 for v in chosen.values())
+    assert len(chosen) == 21 and all(0 <= v <= 5 for v in chosen.values())
     J, K = qb.jk(fb, D, schwarz=0.0, ctx=ctx)
     Jr, Kr = oracle.jk(fb, D, exact=True)
     scale = max(np.abs(Jr).max(), 1.0)

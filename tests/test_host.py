@@ -118,3 +118,36 @@ def test_warp_kernel_configs_fit_shared_memory():
         assert (4 in cfgs) == (nt >= g.BIG_NT), cls
         seen4 += 4 in cfgs
     assert seen4 >= 8
+
+
+def test_segmented_kernel_layout():
+    # the segmented kernel (variant 5): per class with >= 90 targets, its shared memory
+    # (four accumulator rows of emission slots, the HRR buffers, the count tables) fits a
+    # block, and the target -> emission-slot table is a one-to-one map into the rows
+    import importlib.util
+    from pathlib import Path
+    gen = Path(__file__).resolve().parents[1] / "quiqbox.jl_gb300" / "csrc" / "gen_eri.py"
+    spec = importlib.util.spec_from_file_location("gen_eri", gen)
+    g = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(g)
+    seen = 0
+    for cls in g.quartet_classes(2):
+        cg = g.ClassGen(*cls)
+        nt = len(cg.esets) * len(cg.fsets)
+        assert cg.seg == (nt >= g.SEG_MIN_NT)
+        if not cg.seg:
+            continue
+        cg.generate()
+        la, lb, lc, ld = cls
+        nint = g.ncart(la) * g.ncart(lb) * g.ncart(lc) * g.ncart(ld)
+        nab, nf = g.ncart(la) * g.ncart(lb), len(cg.fsets)
+        nr = cg.seg_nbatch * g.SEG_W
+        assert sorted(cg.seg_pos) == sorted(set(cg.seg_pos)) and len(cg.seg_pos) == nt
+        assert 0 <= min(cg.seg_pos) and max(cg.seg_pos) < nr and nr - nt < g.SEG_W
+        wpb = g.seg_warps(cg.seg_nbatch, nab, nf, nint, nt)
+        dyn = wpb * (4 * nr + nab * nf + max(nint, nt)) * 8
+        static = wpb * (32 * 16 * 2 + 5 * 32 * 4 + 32)
+        assert static <= wpb * g.SEG_STATIC_PER_WARP
+        assert dyn + static <= 227 * 1024, cls
+        seen += 1
+    assert seen >= 6
