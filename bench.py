@@ -37,7 +37,7 @@ FLOPS_TABLE = Path(__file__).resolve().parent / "quiqbox.jl_gb300" / "csrc" / "f
 # from one ncu capture of that kernel alone (dram__bytes_read.sum + dram__bytes_write.sum,
 # `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
 #  --kernel-name-base demangled -k regex:<kernel> -c 1 python bench.py --jk-only 1`)
-DOMINANT_TRAFFIC = {}
+DOMINANT_TRAFFIC = {"2111/5": 4437248}
 WORKLOAD = "ERI+J/K: 64 H + 16 C/N/O in a 14 bohr cube, 3-prim Cartesian s/p/d shells, N=416, FP64, Schwarz 1e-12"
 L2_NOTE = ("GPU arm: 256 MiB written before every timed build (L2 flush); "
            "CPU arm: no flush (host caches)")
@@ -343,6 +343,7 @@ def run_ours(args):
         ctx.check(lib.qb_jk_execute(ctx.h))
         ctx.check(lib.qb_jk_get_stats(ctx.h, C.byref(stats)))
     peak = qb.fp64_peak(ctx)
+    dmma_peak = qb.fp64_dmma_peak(ctx)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
     launches_per_step = 3 + sum(1 for c in range(stats.nclass) if stats.class_quartets[c] > 0)
     clocks = ClockSampler(local_rank)
@@ -413,6 +414,10 @@ def run_ours(args):
                          "kernel": f"class ({names[dom][:2]}|{names[dom][2:]}), variant {int(chosen[dom])}",
                          "kernel_ms": float(class_ms[dom]), "flops_per_launch": float(cflops[dom]),
                          "peak_source": "measured: FP64 FMA microbenchmark (qb_fp64_peak) in this run",
+                         "fp64_tensor_peak": dmma_peak,
+                         "fp64_tensor_peak_source": "measured: mma.sync m8n8k4 f64 microbenchmark "
+                                                    "(qb_fp64_dmma_peak) in this run; the integral recursions "
+                                                    "are not matrix products",
                          "flops_source": "per-class FP64 op counts of the generated kernels x this launch's "
                                          "quartets and primitive quartets"},
             "roofline_build": {"achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,

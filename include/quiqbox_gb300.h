@@ -324,6 +324,9 @@ int qb_diis_coefficients(qb_ctx* ctx, int solver, int convex, int m, const doubl
 
 /* Measured FP64 FMA throughput of this device (TFLOP/s), the FP64 roofline denominator. */
 int qb_fp64_peak(qb_ctx* ctx, double* tflops);
+/* Measured FP64 tensor-core throughput of this device (mma.sync m8n8k4 f64, TFLOP/s), for
+ * comparison with qb_fp64_peak (no counterpart in the reference). */
+int qb_fp64_dmma_peak(qb_ctx* ctx, double* tflops);
 
 /* Allocation-free direct J/K (no counterpart in the reference).
  * For callers that cannot allocate device memory themselves (code inside a host

@@ -11,7 +11,7 @@ from .basis import (PrimitiveOrb, CompositeOrb, NuclearCluster, FlatBasis, genGa
                     cartesian_components, norm_factor, basis_set_names, NUCLEAR_CHARGE)
 from .api import (overlaps, overlap, elecKinetics, elecKinetic, nucAttractions, nucAttraction,  # noqa: F401
                   coreHamiltonian, elecRepulsions, elecRepulsion, elecRepulsion_list, jk, SCFconfig,
-                  HFconfig, HFfinalInfo, runHartreeFock, RCHartreeFock, UOHartreeFock, fp64_peak, device_info,
+                  HFconfig, HFfinalInfo, runHartreeFock, RCHartreeFock, UOHartreeFock, fp64_peak, fp64_dmma_peak, device_info,
                   computeBoysSequence, computeBoysFunc, multipoleMoments, multipoleMoment,
                   runHartreeFockBatched, BatchSCFConfig, BatchSCFResult, jk_autotune, diis_coefficients,
                   DimensionMismatch, DomainError)

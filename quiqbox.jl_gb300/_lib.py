@@ -24,7 +24,7 @@ EXPORTED = ["qb_create", "qb_destroy", "qb_last_error", "qb_device_info", "qb_ov
             "qb_batch_config_default", "qb_run_rhf_batched", "qb_jk_autotune",
             "qb_bf16_gemm_nt", "qb_gelu_forward", "qb_gelu_backward", "qb_f32_to_bf16", "qb_bf16_transpose",
             "qb_colsum", "qb_mse_grad", "qb_adam_step", "qb_adjoint_jk", "qb_eigh_lowest",
-            "qb_guess_features", "qb_guess_assemble", "qb_diis_coefficients", "qb_jk_quartet_list", "qb_jk_class_times"]
+            "qb_guess_features", "qb_guess_assemble", "qb_diis_coefficients", "qb_jk_quartet_list", "qb_jk_class_times", "qb_fp64_dmma_peak"]
 
 
 class DimensionMismatch(ValueError):

@@ -549,6 +549,14 @@ def fp64_peak(ctx=None):
     return out.value
 
 
+def fp64_dmma_peak(ctx=None):
+    """Measured FP64 tensor-core (mma.sync m8n8k4) throughput of the device (TFLOP/s)."""
+    c = _ctx(ctx)
+    out = C.c_double()
+    c.check(c.lib.qb_fp64_dmma_peak(c.h, C.byref(out)))
+    return out.value
+
+
 def device_info(ctx=None):
     c = _ctx(ctx)
     sm, ma, mi = C.c_int(), C.c_int(), C.c_int()

@@ -413,6 +413,55 @@ __global__ void qb_dfma_peak_kernel(int iters, double seed, double* sink) {
     if (r == 12345.678) sink[0] = r;
 }
 
+// FP64 tensor-core (DMMA) throughput: mma.sync m8n8k4 f64 (256 FMAs per warp instruction),
+// 8 independent accumulators per warp.
+__global__ void qb_dmma_peak_kernel(int iters, double seed, double* sink) {
+    const double a = seed + threadIdx.x * 1e-3, b = 0.999999 + threadIdx.x * 1e-9;
+    double c[8][2];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        c[k][0] = k;
+        c[k][1] = k + 0.5;
+    }
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                             : "+d"(c[k][0]), "+d"(c[k][1])
+                             : "d"(a), "d"(b));
+    }
+    double r = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) r += c[k][0] + c[k][1];
+    if (r == 12345.678) sink[0] = r;
+}
+
+extern "C" int qb_fp64_dmma_peak(qb_ctx* ctx, double* tflops) {
+    QB_TRY(enter(ctx));
+    if (!tflops) return qb_set_error(ctx, QB_ERR_ARG, "null output");
+    DevArray<double> sink;
+    QB_CUDA(ctx, sink.ensure(1));
+    const int block = 256, grid = ctx->nsm * 8, iters = 1000;
+    qb_dmma_peak_kernel<<<grid, block, 0, ctx->stream>>>(16, 1.0, sink.p);   // warm-up
+    QB_CUDA(ctx, cudaGetLastError());
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; ++rep) {
+        QB_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
+        qb_dmma_peak_kernel<<<grid, block, 0, ctx->stream>>>(iters, 1.0 + rep, sink.p);
+        QB_CUDA(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
+        QB_CUDA(ctx, cudaEventSynchronize(ctx->ev_stop));
+        float ms = 0.f;
+        QB_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+        if (ms < best) best = ms;
+    }
+    const double flops = 512.0 * 4.0 * 8.0 * (double)iters * (double)(block / 32) * (double)grid;
+    *tflops = flops / (best * 1e-3) / 1e12;
+    sink.release();
+    return QB_OK;
+}
+
 extern "C" int qb_fp64_peak(qb_ctx* ctx, double* tflops) {
     QB_TRY(enter(ctx));
     if (!tflops) return qb_set_error(ctx, QB_ERR_ARG, "null output");

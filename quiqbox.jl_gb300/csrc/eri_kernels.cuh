@@ -520,6 +520,23 @@ __device__ __forceinline__ void qb_rs8_add(double* row, int j8, double v0, doubl
     row[j8] += c;
 }
 
+// The same reduce-scatter through shared memory: every lane stores its eight values in its
+// own row of the warp's staging area (rows of 9 doubles, so that the reads below spread over
+// the banks), the warp synchronises, and lane j8 sums value j8 of the eight rows of its
+// segment and adds the sum to row[j8].  Eight FP64 adds per eight values, as the shuffle
+// form, but about half its instructions.  Two staging areas alternate by batch parity, so
+// one warp synchronisation per batch orders every store after the reads of the batch that
+// last used the area.
+__device__ __forceinline__ void qb_stage8_add(double* stage, double* row, int lane, int j8, double v0, double v1,
+                                             double v2, double v3, double v4, double v5, double v6, double v7) {
+    double* my = stage + lane * 9;
+    my[0] = v0; my[1] = v1; my[2] = v2; my[3] = v3; my[4] = v4; my[5] = v5; my[6] = v6; my[7] = v7;
+    __syncwarp();
+    const double* sg = stage + (lane & ~7) * 9 + j8;
+    const double s = ((sg[0] + sg[9]) + (sg[18] + sg[27])) + ((sg[36] + sg[45]) + (sg[54] + sg[63]));
+    row[j8] += s;
+}
+
 #define QB_SEG_MAXNB 16   // bra primitive pairs whose ket counts the segmented kernel tabulates
 
 // Segmented kernel (classes with many contracted targets).  A warp takes a batch of G <= 32
@@ -538,7 +555,8 @@ template <class C>
 struct QbSeg {
     static constexpr int NR = C::NSEGB * 8;   // row length: emission slots of the targets
     static constexpr int NI = C::NINT > C::NT ? C::NINT : C::NT;
-    static constexpr int doubles = 4 * NR + C::NA * C::NB * C::NF + NI;   // per warp
+    static constexpr int STAGE = 2 * 32 * 9;    // two staging areas of the reduce-scatter
+    static constexpr int doubles = 4 * NR + C::NA * C::NB * C::NF + NI + STAGE;   // per warp
 };
 
 template <int LA, int LB, int LC, int LD, int WPB>
@@ -556,6 +574,7 @@ __global__ void __launch_bounds__(32 * WPB) qb_jk_seg_kernel(const ClassWork w, 
     double* rows = qb_dyn_smem + (size_t)warp * QbSeg<C>::doubles;
     double* Tb = rows + 4 * NR;    // (ab|f) of the current owner, [ab][f]
     double* Ib = Tb + NAB * NF;    // the owner's targets in (e, f) order, then its (ab|cd) block
+    double* stage = Ib + QbSeg<C>::NI;   // reduce-scatter staging, two areas
     const long long total = __ldg(w.offs + w.nbra);
     const long long nwarps = (long long)gridDim.x * WPB;
     // owners per batch: a multiple of 4 in [4, 32], about a sixth of the quartets per warp
@@ -644,7 +663,10 @@ __global__ void __launch_bounds__(32 * WPB) qb_jk_seg_kernel(const ClassWork w, 
                 if (!act) B.K = 0.0;   // zero prefactor: every target of this lane is zero
                 C::prim_seg(B, Kt, a.boys,
                             [&](int b, double v0, double v1, double v2, double v3, double v4, double v5, double v6,
-                                double v7) { qb_rs8_add(row + 8 * b, j8, v0, v1, v2, v3, v4, v5, v6, v7); });
+                                double v7) {
+                                qb_stage8_add(stage + (b & 1) * (32 * 9), row + 8 * b, lane, j8, v0, v1, v2, v3, v4,
+                                              v5, v6, v7);
+                            });
             }
             if (j8 == 0) nprim += tot;
             __syncwarp();

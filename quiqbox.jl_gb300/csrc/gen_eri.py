@@ -533,6 +533,7 @@ PREFERRED = {"2211": 5, "2221": 5, "2111": 5, "2121": 5, "2220": 4, "2222": 4,
 SEG_W = 8
 SEG_MIN_NT = 90
 SEG_STATIC_PER_WARP = 2560     # bytes of static shared memory per warp (tables) in qb_jk_seg_kernel
+SEG_STAGE = 2 * 32 * 9         # doubles per warp of the reduce-scatter staging areas
 SMEM_LIMIT = 227 * 1024
 
 
@@ -540,7 +541,7 @@ def seg_warps(nsegb, nab, nf, nint, nt):
     """Warps per block of the segmented kernel: as many as shared memory allows, at most 8,
     and 4 for the classes of >= 400 targets (at 8 warps ptxas gives their VRR 32 registers
     and keeps everything else in local memory; at 4 it uses 255)."""
-    per_warp = 8 * (4 * nsegb * SEG_W + nab * nf + max(nint, nt)) + SEG_STATIC_PER_WARP
+    per_warp = 8 * (4 * nsegb * SEG_W + nab * nf + max(nint, nt) + SEG_STAGE) + SEG_STATIC_PER_WARP
     return max(1, min(8 if nt < 400 else 4, SMEM_LIMIT // per_warp))
 
 
