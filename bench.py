@@ -37,7 +37,7 @@ FLOPS_TABLE = Path(__file__).resolve().parent / "quiqbox.jl_gb300" / "csrc" / "f
 # from one ncu capture of that kernel alone (dram__bytes_read.sum + dram__bytes_write.sum,
 # `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
 #  --kernel-name-base demangled -k regex:<kernel> -c 1 python bench.py --jk-only 1`)
-DOMINANT_TRAFFIC = {"2111/5": 4437248}
+DOMINANT_TRAFFIC = {"2111/5": 4431616}
 WORKLOAD = "ERI+J/K: 64 H + 16 C/N/O in a 14 bohr cube, 3-prim Cartesian s/p/d shells, N=416, FP64, Schwarz 1e-12"
 L2_NOTE = ("GPU arm: 256 MiB written before every timed build (L2 flush); "
            "CPU arm: no flush (host caches)")
@@ -687,6 +687,8 @@ def run_jk_only(args):
     classes = {"".join(str(v) for v in st.class_l[c]): [st.class_quartets[c], st.class_prim_quartets[c]]
                for c in range(st.nclass)}
     print(json.dumps({"class_quartets_prim_quartets": classes}), flush=True)
+    print(json.dumps({"fp64_fma_peak_tflops": qb.fp64_peak(ctx), "fp64_dmma_peak_tflops": qb.fp64_dmma_peak(ctx)}),
+          flush=True)
 
 
 def run_tune_only(args):

@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(128) qb_batch_store_kernel(const BatchWork w, 
         const ShellPair Q = w.ket[j];
         double I[C::NINT];
         C::block(prims + P.prim0, P.nprim, prims + Q.prim0, Q.nprim, P.ABx, P.ABy, P.ABz, Q.ABx, Q.ABy, Q.ABz, boys,
-                 I, nprimq);
+                 I, nprimq, (float)QB_PRIM_EPS_Q);
 #pragma unroll
         for (int k = 0; k < C::NINT; ++k) out[(size_t)k * total + t] = I[k];
     }
@@ -1069,6 +1069,32 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
         QB_CUDA(ctx, cudaGetLastError());
     }
     QB_TRY(qb_check_status(ctx));
+    // primitive Schwarz keys (as in the single-basis J/K engine): each primitive pair's
+    // screening key becomes its own Schwarz factor, the primitives of a shell pair are
+    // re-sorted by it and the negligible ones dropped; the stores then skip primitive
+    // quartets whose keys multiply to < QB_PRIM_EPS_Q
+    {
+        DevArray<unsigned> d_keymax;
+        QB_CUDA(ctx, d_keymax.ensure(1));
+        QB_CUDA(ctx, cudaMemsetAsync(d_keymax.p, 0, sizeof(unsigned), s));
+        for (int pc = 0; pc < npc; ++pc) {
+            const int n = pc_off[pc + 1] - pc_off[pc];
+            if (n == 0) continue;
+            const ShellPair* pp = d_pairs.p + pc_off[pc];
+            const int g = (n + 127) / 128;
+            if (pc == 0) qb_prim_key_kernel<0, 0><<<g, 128, 0, s>>>(pp, n, d_prims.p, ctx->boys.p, d_keymax.p);
+            else if (pc == 1) qb_prim_key_kernel<1, 0><<<g, 128, 0, s>>>(pp, n, d_prims.p, ctx->boys.p, d_keymax.p);
+            else qb_prim_key_kernel<1, 1><<<g, 128, 0, s>>>(pp, n, d_prims.p, ctx->boys.p, d_keymax.p);
+            QB_CUDA(ctx, cudaGetLastError());
+        }
+        if (qb_compact_prim_keys(s, d_pairs.p, npair, d_prims.p, d_prims32.p, nslot, d_keymax.p,
+                                 (float)QB_PRIM_EPS_Q, d_nkept.p) != 0)
+            return qb_cuda_check(ctx, cudaGetLastError(), "batched primitive Schwarz keys");
+        std::vector<int> nkept(npair);
+        QB_CUDA(ctx, cudaMemcpyAsync(nkept.data(), d_nkept.p, npair * sizeof(int), cudaMemcpyDeviceToHost, s));
+        QB_CUDA(ctx, cudaStreamSynchronize(s));
+        for (int k = 0; k < npair; ++k) pairs[k].nprim = nkept[k];
+    }
     {
         std::vector<double> Q(npair);
         QB_CUDA(ctx, cudaMemcpyAsync(Q.data(), d_Q.p, npair * sizeof(double), cudaMemcpyDeviceToHost, s));

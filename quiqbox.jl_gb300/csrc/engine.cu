@@ -300,6 +300,18 @@ __global__ void qb_primpair_f32_kernel(const PrimPair* __restrict__ prims, int n
     out[k] = make_float4((float)r.p, (float)r.Px, (float)r.Py, (float)r.Pz);
 }
 
+// After the primitive Schwarz keys are in place (qb_prim_key_kernel per pair class, their
+// maximum in *d_keymax): sort and compact every shell pair's primitive pairs by key (nkept)
+// and refresh the FP32 centres in the new order.
+int qb_compact_prim_keys(cudaStream_t s, const ShellPair* d_pairs, int npair, PrimPair* d_prims, float4* d_prims32,
+                         int nslot, const unsigned* d_keymax, float eps, int* d_nkept) {
+    if (npair > 0)
+        qb_primpair_key_compact_kernel<<<(npair + 127) / 128, 128, 0, s>>>(d_pairs, npair, d_prims, d_keymax, eps,
+                                                                            d_nkept);
+    if (nslot > 0) qb_primpair_f32_kernel<<<(nslot + 127) / 128, 128, 0, s>>>(d_prims, nslot, d_prims32);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 // Primitive pairs of every slot, sorted and compacted per shell pair (nkept), plus their
 // FP32 centres.  d_kmax is scratch (one word).
 int qb_build_prim_pairs(cudaStream_t s, const PairSlot* d_slots, int nslot, const double* d_cen,
@@ -423,13 +435,9 @@ int qb_ensure_pairs(qb_ctx* ctx) {
             if (!launch) return qb_set_error(ctx, QB_ERR_UNSUPPORTED, "no diagonal class for a pair class");
             launch(ctx->d_pairs.p + ctx->pc_off[pc], n, ctx->d_prims.p, ctx->boys.p, d_keymax.p, s);
         }
-        if (npair > 0)
-            qb_primpair_key_compact_kernel<<<(npair + 127) / 128, 128, 0, s>>>(ctx->d_pairs.p, npair, ctx->d_prims.p,
-                                                                                d_keymax.p, ctx->prim_eps,
-                                                                                d_nkept.p);
-        if (nslot > 0)
-            qb_primpair_f32_kernel<<<(nslot + 127) / 128, 128, 0, s>>>(ctx->d_prims.p, nslot, ctx->d_prims32.p);
-        QB_CUDA(ctx, cudaGetLastError());
+        if (qb_compact_prim_keys(s, ctx->d_pairs.p, npair, ctx->d_prims.p, ctx->d_prims32.p, nslot, d_keymax.p,
+                                 ctx->prim_eps, d_nkept.p) != 0)
+            return qb_cuda_check(ctx, cudaGetLastError(), "primitive Schwarz keys");
         std::vector<int> nkept(npair);
         QB_CUDA(ctx, cudaMemcpyAsync(nkept.data(), d_nkept.p, npair * sizeof(int), cudaMemcpyDeviceToHost, s));
         QB_CUDA(ctx, cudaStreamSynchronize(s));

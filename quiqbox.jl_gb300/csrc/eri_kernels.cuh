@@ -556,7 +556,10 @@ struct QbSeg {
     static constexpr int NR = C::NSEGB * 8;   // row length: emission slots of the targets
     static constexpr int NI = C::NINT > C::NT ? C::NINT : C::NT;
     static constexpr int STAGE = 2 * 32 * 9;    // two staging areas of the reduce-scatter
-    static constexpr int doubles = 4 * NR + C::NA * C::NB * C::NF + NI + STAGE;   // per warp
+    static constexpr int HRRBUF = C::NA * C::NB * C::NF + NI;
+    // per warp: four rows, then the HRR buffers, which the staging areas share (the rounds
+    // and the HRR phase of a wave never overlap)
+    static constexpr int doubles = 4 * NR + (HRRBUF > STAGE ? HRRBUF : STAGE);
 };
 
 template <int LA, int LB, int LC, int LD, int WPB>
@@ -574,7 +577,7 @@ __global__ void __launch_bounds__(32 * WPB) qb_jk_seg_kernel(const ClassWork w, 
     double* rows = qb_dyn_smem + (size_t)warp * QbSeg<C>::doubles;
     double* Tb = rows + 4 * NR;    // (ab|f) of the current owner, [ab][f]
     double* Ib = Tb + NAB * NF;    // the owner's targets in (e, f) order, then its (ab|cd) block
-    double* stage = Ib + QbSeg<C>::NI;   // reduce-scatter staging, two areas
+    double* stage = Tb;            // reduce-scatter staging (two areas) during the rounds
     const long long total = __ldg(w.offs + w.nbra);
     const long long nwarps = (long long)gridDim.x * WPB;
     // owners per batch: a multiple of 4 in [4, 32], about a sixth of the quartets per warp

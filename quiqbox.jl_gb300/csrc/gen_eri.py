@@ -541,7 +541,7 @@ def seg_warps(nsegb, nab, nf, nint, nt):
     """Warps per block of the segmented kernel: as many as shared memory allows, at most 8,
     and 4 for the classes of >= 400 targets (at 8 warps ptxas gives their VRR 32 registers
     and keeps everything else in local memory; at 4 it uses 255)."""
-    per_warp = 8 * (4 * nsegb * SEG_W + nab * nf + max(nint, nt) + SEG_STAGE) + SEG_STATIC_PER_WARP
+    per_warp = 8 * (4 * nsegb * SEG_W + max(nab * nf + max(nint, nt), SEG_STAGE)) + SEG_STATIC_PER_WARP
     return max(1, min(8 if nt < 400 else 4, SMEM_LIMIT // per_warp))
 
 

@@ -81,6 +81,8 @@ struct PairSlot {
 int qb_build_prim_pairs(cudaStream_t s, const PairSlot* d_slots, int nslot, const double* d_cen,
                         const double* d_alpha, const double* d_w, const ShellPair* d_pairs, int npair,
                         PrimPair* d_prims, float4* d_prims32, int* d_nkept, unsigned long long* d_kmax);
+int qb_compact_prim_keys(cudaStream_t s, const ShellPair* d_pairs, int npair, PrimPair* d_prims, float4* d_prims32,
+                         int nslot, const unsigned* d_keymax, float eps, int* d_nkept);
 
 int qb_jk_autotune_device(qb_ctx* ctx, int repeats, int* chosen);
 int qb_jk_class_times_device(qb_ctx* ctx, int repeats, float* ms);

@@ -145,7 +145,7 @@ def test_segmented_kernel_layout():
         assert sorted(cg.seg_pos) == sorted(set(cg.seg_pos)) and len(cg.seg_pos) == nt
         assert 0 <= min(cg.seg_pos) and max(cg.seg_pos) < nr and nr - nt < g.SEG_W
         wpb = g.seg_warps(cg.seg_nbatch, nab, nf, nint, nt)
-        dyn = wpb * (4 * nr + nab * nf + max(nint, nt) + g.SEG_STAGE) * 8
+        dyn = wpb * (4 * nr + max(nab * nf + max(nint, nt), g.SEG_STAGE)) * 8
         static = wpb * (32 * 16 * 2 + 5 * 32 * 4 + 32)
         assert static <= wpb * g.SEG_STATIC_PER_WARP
         assert dyn + static <= 227 * 1024, cls
