@@ -289,6 +289,9 @@ typedef struct {
     double oscillate_threshold;  /* default 5e-6                                                 */
     int early_stop;         /* default 1                                                          */
     double damp_strength;   /* DD damping, default 0.75                                           */
+    int digest_chunk;       /* stored quartets per digest block of a molecule with much work in a
+                               class (a quarter of it for the others); 0 (default): chosen by timing
+                               on the batch                                                          */
 } qb_batch_config;
 
 typedef struct {

@@ -173,7 +173,8 @@ class QBBatchConfig(C.Structure):
                 ("initial_density", C.POINTER(C.c_double)), ("eigensolver", C.c_int), ("jacobi_sweeps", C.c_int),
                 ("fallback_iter", C.c_int), ("nmethod", C.c_int), ("method", C.c_int * 8),
                 ("interval", C.c_double * 8), ("solver", C.c_int * 8), ("secondary_ratio", C.c_double * 2),
-                ("oscillate_threshold", C.c_double), ("early_stop", C.c_int), ("damp_strength", C.c_double)]
+                ("oscillate_threshold", C.c_double), ("early_stop", C.c_int), ("damp_strength", C.c_double),
+                ("digest_chunk", C.c_int)]
 
 
 class QBBatchResult(C.Structure):

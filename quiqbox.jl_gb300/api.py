@@ -402,6 +402,7 @@ class BatchSCFConfig:
                                            # else the reference's method sequence, e.g. SCFconfig.default(1e-10)
     earlyStop: bool = True
     dampStrength: float = 0.75
+    digest_chunk: int = 0         # stored quartets per digest block (0: chosen by timing on the batch)
 
 
 @dataclass
@@ -508,6 +509,7 @@ def runHartreeFockBatched(molecules, config: Optional[BatchSCFConfig] = None, ct
     qcfg.initial_density = L.dptr(d0) if d0 is not None else d0_dev
     qcfg.eigensolver, qcfg.jacobi_sweeps, qcfg.fallback_iter = cfg.eigensolver, cfg.jacobi_sweeps, cfg.fallback_iter
     qcfg.early_stop, qcfg.damp_strength = int(bool(cfg.earlyStop)), float(cfg.dampStrength)
+    qcfg.digest_chunk = int(cfg.digest_chunk)
     if cfg.strategy is not None:
         st = cfg.strategy
         if len(st.methods) > 8:

@@ -98,7 +98,8 @@ struct StepParams {
     double r1, r2, osc, damp;          // secondaryConvRatio, oscillateThreshold, dampStrength
     int max_iter, diis, early_stop;
     int sweeps, eig;                   // eig 0: tridiagonal occupied-subspace solver, 1: Jacobi
-    int fallback;                      // > 0: restart from the core-Hamiltonian guess after this many
+    int fallback;                      // > 0: restart from the core-Hamiltonian guess after this many iterations
+    int need_df;                       // some method is EDIIS or ADIIS: keep the <D_a, F_b> Gram entries
 };
 
 // ---------------------------------------------------------------------------
@@ -516,7 +517,10 @@ __global__ void __launch_bounds__(QB_BATCH_THREADS) qb_batch_step_kernel(MolDev*
     dd = qb_cta_sum(dd, red);
     const double rmsD = 2.0 * sqrt(dd) / n;   // RMS change of the total density 2D (rmsOf, src/Tools.jl:588)
     const int nl = s_nlive;
-    for (int k = tid >> 5; k < 3 * nl; k += nt >> 5) {   // one warp per Gram entry
+    // one warp per Gram entry: <e'_new, e'_o> always, <D, F> both ways only when a method of the
+    // strategy (EDIIS, ADIIS) uses them
+    const int nkind = prm.need_df ? 3 : 1;
+    for (int k = tid >> 5; k < nkind * nl; k += nt >> 5) {
         const int o = s_idx[k % nl], kind = k / nl;
         const double* a = kind == 0 ? Es : (kind == 1 ? Ds : M.Ds + (size_t)o * nn);
         const double* b = kind == 0 ? M.Es + (size_t)o * nn : (kind == 1 ? M.Fs + (size_t)o * nn : Fs);
@@ -830,6 +834,7 @@ extern "C" void qb_batch_config_default(qb_batch_config* cfg) {
     cfg->oscillate_threshold = 5e-6;
     cfg->early_stop = 1;
     cfg->damp_strength = 0.75;
+    cfg->digest_chunk = 0;
 }
 
 int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nnuc, const double* Z,
@@ -840,7 +845,7 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     if (cfg_in) cfg = *cfg_in;
     else qb_batch_config_default(&cfg);
     if (cfg.diis_size < 1 || cfg.diis_size > QB_BATCH_DIIS || cfg.max_iter < 1 || cfg.iters_per_graph < 1 ||
-        cfg.fallback_iter < 0 ||
+        cfg.fallback_iter < 0 || cfg.digest_chunk < 0 ||
         !(cfg.schwarz >= 0.0) || !(cfg.conv_energy > 0.0) || !(cfg.conv_density > 0.0))
         return qb_set_error(ctx, QB_ERR_DOMAIN, "bad batched SCF configuration");
     if (cfg.nmethod < 0 || cfg.nmethod > 8) return qb_set_error(ctx, QB_ERR_ARG, "nmethod must be 0..8");
@@ -1211,11 +1216,17 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     static const long long kChunkCand[3][2] = {{QB_DIGEST_CHUNK / 2, QB_DIGEST_CHUNK_SMALL / 2},
                                                {QB_DIGEST_CHUNK, QB_DIGEST_CHUNK_SMALL},
                                                {2 * QB_DIGEST_CHUNK, 2 * QB_DIGEST_CHUNK_SMALL}};
-    build_chunks(kChunkCand[0][0], kChunkCand[0][1]);   // the finest split has the most chunks
+    // size the chunk table for the finest split that may be used
+    if (cfg.digest_chunk > 0 && cfg.digest_chunk < kChunkCand[0][0])
+        build_chunks(cfg.digest_chunk, std::max(1LL, (long long)cfg.digest_chunk / 4));
+    else
+        build_chunks(kChunkCand[0][0], kChunkCand[0][1]);
     DevArray<DigestChunk> d_chunks;
     QB_CUDA(ctx, d_chunks.ensure(std::max<size_t>(1, h_chunks.size())));
     int best_cand = 1;
-    {
+    if (cfg.digest_chunk > 0) {
+        best_cand = -1;   // fixed by the caller
+    } else {
         QB_CUDA(ctx, cudaMemsetAsync(d_mats.p + 5 * (size_t)NN, 0, NN * sizeof(double), s));   // D~
         float best_ms = -1.f;
         for (int k = 0; k < 3; ++k) {
@@ -1240,7 +1251,9 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
         }
         QB_CUDA(ctx, cudaMemsetAsync(d_mats.p + 7 * (size_t)NN, 0, 2 * NN * sizeof(double), s));   // J', K'
     }
-    build_chunks(kChunkCand[best_cand][0], kChunkCand[best_cand][1]);
+    const long long chunk_big = best_cand >= 0 ? kChunkCand[best_cand][0] : (long long)cfg.digest_chunk;
+    const long long chunk_small = best_cand >= 0 ? kChunkCand[best_cand][1] : std::max(1LL, chunk_big / 4);
+    build_chunks(chunk_big, chunk_small);
     if (!h_chunks.empty())
         QB_CUDA(ctx, cudaMemcpyAsync(d_chunks.p, h_chunks.data(), h_chunks.size() * sizeof(DigestChunk),
                                      cudaMemcpyHostToDevice, s));
@@ -1287,6 +1300,8 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
         prm.early_stop = cfg.early_stop;
         prm.damp = cfg.damp_strength;
     }
+    for (int l = 0; l < prm.nmethod; ++l)
+        if (prm.method[l] == QB_SCF_EDIIS || prm.method[l] == QB_SCF_ADIIS) prm.need_df = 1;
     prm.max_iter = cfg.max_iter;
     prm.diis = std::max(2, cfg.diis_size);
     prm.sweeps = cfg.jacobi_sweeps > 0 ? std::min(cfg.jacobi_sweeps, 60) : 60;
@@ -1396,7 +1411,7 @@ int qb_batch_rhf_run(qb_ctx* ctx, int nmol, const qb_basis* bases, const int* nn
     res->prim_quartets = (int64_t)nprimq;
     res->eri_doubles = (int64_t)eri_at[QB_BATCH_NCLASS];
     res->graph_launches = launches;
-    res->digest_chunk = (int)kChunkCand[best_cand][0];
+    res->digest_chunk = (int)chunk_big;
     int failed = 0;
     for (int m = 0; m < nmol; ++m) {
         if (res->energy) res->energy[m] = hm[m].E;
