@@ -520,6 +520,14 @@ def config0(qb, oracle, solves=20):
     for _ in range(solves):
         r = qb.runHartreeFock(nuc, fb, cfg)
     t_gpu = (time.perf_counter() - t0) / solves
+    # the same solve through the batched engine (one molecule; whole SCF in one graph launch)
+    bcfg = qb.BatchSCFConfig(strategy=qb.SCFconfig(("DIIS",), (1e-10,), secondaryConvRatio=(1e6, 100.0)))
+    for _ in range(2):
+        rb = qb.runHartreeFockBatched([(nuc, fb, 0)], config=bcfg)
+    t0 = time.perf_counter()
+    for _ in range(solves):
+        rb = qb.runHartreeFockBatched([(nuc, fb, 0)], config=bcfg)
+    t_bat = (time.perf_counter() - t0) / solves
     ro = oracle.hartree_fock(fb, nuc.charges, nuc.positions, 5, 5, guess="CoreH", methods=("DIIS",),
                              intervals=(1e-10,), secondary=(1e6, 100.0))
     t0 = time.perf_counter()
@@ -532,6 +540,8 @@ def config0(qb, oracle, solves=20):
             "gpu_solves_per_s": 1.0 / t_gpu, "gpu_ms_per_solve": 1e3 * t_gpu, "iterations": int(r.steps),
             "converged": bool(r.converged), "E_total": float(sum(r.energy)),
             "abs_dE_vs_oracle": float(abs(r.energy[0] - ro["E_elec"])),
+            "gpu_batched_engine_ms_per_solve": 1e3 * t_bat, "gpu_batched_engine_iterations": int(rb.iterations[0]),
+            "gpu_batched_engine_abs_dE_vs_oracle": float(abs(rb.elec_energies[0] - ro["E_elec"])),
             "oracle_iterations": int(ro["steps"]),
             "cpu_solves_per_s": 1.0 / t_cpu, "cpu_ms_per_solve": 1e3 * t_cpu,
             "cpu_kind": "port (oracle restatement of runHartreeFock, stored ERI tensor)",
