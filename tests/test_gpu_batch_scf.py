@@ -90,6 +90,22 @@ def test_batched_rhf_matches_single_molecule_path(qb):
         assert abs(res.elec_energies[k] - r.energy[0]) < 1e-10
 
 
+def test_batched_rhf_fixed_digest_chunk(qb):
+    # a caller-fixed digest chunk (qb_batch_config.digest_chunk) changes only how the stored
+    # quartets are split into blocks: same converged energies as the timed choice
+    from quiqbox_gb300.workloads import batch_molecules
+    mols = batch_molecules(16, seed=9, atoms=(2, 8))
+    args = [(m["nuc"], m["flat"], m["charge"]) for m in mols]
+    auto = qb.runHartreeFockBatched(args)
+    fixed = qb.runHartreeFockBatched(args, config=qb.BatchSCFConfig(digest_chunk=256))
+    assert fixed.digest_chunk == 256
+    both = auto.converged & fixed.converged
+    assert both.sum() >= 12
+    assert np.abs(auto.elec_energies[both] - fixed.elec_energies[both]).max() < 1e-10
+    with pytest.raises(Exception):
+        qb.runHartreeFockBatched(args[:2], config=qb.BatchSCFConfig(digest_chunk=-1))
+
+
 def test_batched_rhf_full_workload_sizes(qb, oracle):
     # the benchmark's molecule generator at full size range (2-16 atoms, 2-120 functions).
     # Pure DIIS from the core-Hamiltonian guess does not converge every random chain in 200

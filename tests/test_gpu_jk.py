@@ -182,6 +182,60 @@ def test_jk_autotune_keeps_results(qb, oracle):
     assert np.abs(K - Kr).max() < 1e-12 * scale
 
 
+def test_class_times_and_fp64_peaks(qb, oracle):
+    # the measurement hooks: every class kernel timed alone (positive for the classes with
+    # work), J and K unchanged afterwards; both FP64 microbenchmarks report a rate
+    import ctypes as C
+    from quiqbox_gb300 import _lib as L
+    fb, D = _small_shell_system(qb, 1, n_h=2, n_heavy=1, box=4.0)
+    ctx = qb.Context(0)
+    b = L.BasisArgs(fb)
+    Df = np.ascontiguousarray(D.reshape(-1, order="F"))
+    ctx.check(ctx.lib.qb_jk_prepare(ctx.h, b.ref(), 0.0))
+    ctx.check(ctx.lib.qb_jk_upload_density(ctx.h, L.dptr(Df)))
+    ctx.check(ctx.lib.qb_jk_execute(ctx.h))
+    st = L.QBJKStats()
+    ctx.check(ctx.lib.qb_jk_get_stats(ctx.h, C.byref(st)))
+    ms = np.zeros(32, np.float32)
+    ctx.check(ctx.lib.qb_jk_class_times(ctx.h, 2, ms.ctypes.data_as(C.POINTER(C.c_float))))
+    for c in range(st.nclass):
+        assert (ms[c] > 0) == (st.class_quartets[c] > 0), c
+    n = fb.nfun
+    J, K = np.zeros(n * n), np.zeros(n * n)
+    ctx.check(ctx.lib.qb_jk_download(ctx.h, L.dptr(J), L.dptr(K)))
+    Jr, Kr = oracle.jk(fb, D, exact=True)
+    scale = max(np.abs(Jr).max(), 1.0)
+    assert np.abs(J.reshape((n, n), order="F") - Jr).max() < 1e-12 * scale
+    assert np.abs(K.reshape((n, n), order="F") - Kr).max() < 1e-12 * scale
+    assert 0.1 < qb.fp64_peak(ctx) < 100.0
+    assert 0.1 < qb.fp64_dmma_peak(ctx) < 100.0
+
+
+def test_primitive_threshold_override(qb, oracle, tmp_path):
+    # QB_JK_PRIM_EPS=0 evaluates every primitive quartet (no primitive Schwarz screening);
+    # J and K stay exact with and without the default screening
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    out = tmp_path / "jk_eps0.npz"
+    env = dict(os.environ, QB_JK_PRIM_EPS="0")
+    subprocess.run([sys.executable, "-c", _VARIANT_SCRIPT, str(out)], cwd=root, env=env, check=True, timeout=600)
+    got = np.load(out)
+    from quiqbox_gb300.workloads import random_shell_molecule, random_density
+    kw = dict(n_h=2, n_heavy=1, box=4.0, min_dist=1.0, seed=0)
+    atoms, coords, bs = random_shell_molecule(**kw)
+    fb = qb.flatten(bs)
+    D = random_density(fb.nfun, kw["seed"])
+    Jr, Kr = oracle.jk(fb, D, exact=True)
+    J, K = qb.jk(fb, D, schwarz=0.0)
+    scale = max(np.abs(Jr).max(), 1.0)
+    for Jx, Kx in ((got["classes_J"], got["classes_K"]), (J, K)):
+        assert np.abs(Jx - Jr).max() < 1e-12 * scale
+        assert np.abs(Kx - Kr).max() < 1e-12 * scale
+
+
 # ---------------------------------------------------------------------------
 # Parity at the bench workload's own size and screening (64 H + 16 heavy atoms, N = 416,
 # Schwarz 1e-12, primitive-quartet screening on): the production class kernels evaluated
