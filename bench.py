@@ -37,7 +37,7 @@ FLOPS_TABLE = Path(__file__).resolve().parent / "quiqbox.jl_gb300" / "csrc" / "f
 # from one ncu capture of that kernel alone (dram__bytes_read.sum + dram__bytes_write.sum,
 # `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
 #  --kernel-name-base demangled -k regex:<kernel> -c 1 python bench.py --jk-only 1`)
-DOMINANT_TRAFFIC = {"2111/5": 4431616}
+DOMINANT_TRAFFIC = {"2111/5": 4412416}
 WORKLOAD = "ERI+J/K: 64 H + 16 C/N/O in a 14 bohr cube, 3-prim Cartesian s/p/d shells, N=416, FP64, Schwarz 1e-12"
 L2_NOTE = ("GPU arm: 256 MiB written before every timed build (L2 flush); "
            "CPU arm: no flush (host caches)")
