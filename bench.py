@@ -336,7 +336,7 @@ def run_ours(args):
     # per-class kernel variant chosen by timing on this workload (autotuned quartet kernels)
     chosen = np.zeros(32, np.int32)
     t_tune = time.perf_counter()
-    ctx.check(lib.qb_jk_autotune(ctx.h, 1, L.iptr(chosen)))
+    ctx.check(lib.qb_jk_autotune(ctx.h, 2, L.iptr(chosen)))
     t_tune = time.perf_counter() - t_tune
     stats = L.QBJKStats()
     for _ in range(args.warmup):
