@@ -78,6 +78,23 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
 
+def max_over_ranks(values, dist=None, device="cpu"):
+    """Element-wise maximum of per-rank timings over all ranks (the replicas' whole-job time
+    is the slowest rank's); the values themselves on a single process."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
+def replica_throughput(world, quartets, steps, seconds):
+    """Whole-job GQuartet/s of `world` replicas, each building `steps` times a workload of
+    `quartets` shell quartets, the slowest taking `seconds`."""
+    return world * quartets * steps / seconds / 1e9
+
+
 # ---------------------------------------------------------------------------
 class ClockSampler:
     """nvidia-smi clock / throttle-reason samples during the timed region."""
@@ -373,14 +390,9 @@ def run_ours(args):
         t0 = time.perf_counter()
         ctx.check(lib.qb_jk(ctx.h, b.ref(), L.dptr(Dp), args.schwarz, L.dptr(Jp), L.dptr(Kp)))
         e2e_s.append(time.perf_counter() - t0)
-    if dist:
-        t = torch.tensor([total_ms, float(np.sum(e2e_s))], dtype=torch.float64, device=f"cuda:{local_rank}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, e2e_tot = float(t[0]), float(t[1])
-    else:
-        e2e_tot = float(np.sum(e2e_s))
-    value = world * q * args.steps / (total_ms * 1e-3) / 1e9
-    e2e_value = world * q * args.steps / e2e_tot / 1e9
+    total_ms, e2e_tot = max_over_ranks([total_ms, float(np.sum(e2e_s))], dist, f"cuda:{local_rank}")
+    value = replica_throughput(world, q, args.steps, total_ms * 1e-3)
+    e2e_value = replica_throughput(world, q, args.steps, e2e_tot)
     achieved = float(np.mean(flops)) / (total_ms / args.steps * 1e-3) / 1e12
     # the dominant kernel: every class kernel timed alone (CUDA events on the library's
     # stream), flops from the generated per-class operation counts
