@@ -165,6 +165,7 @@ int qb_set_basis(qb_ctx* ctx, const qb_basis* b) {
     ctx->basis_valid = false;
     ctx->pairs_valid = false;
     ctx->jk_prepared = false;
+    for (int c = 0; c < QB_MAX_CLASS; ++c) ctx->class_ms[c] = 0.f;   // timings belong to the old basis
     ctx->nfun = nf;
     ctx->nprim = np;
     ctx->h_fp.assign(b->fun_ptr, b->fun_ptr + nf + 1);
@@ -616,15 +617,30 @@ int qb_jk_device(qb_ctx* ctx, const double* dD, double* dJ, double* dK, double t
     QB_CUDA(ctx, cudaMemsetAsync(ctx->d_primcount.p, 0, QB_MAX_CLASS * sizeof(unsigned long long), s));
     QB_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
     for (int k2 = 0; k2 < QB_NSTREAM; ++k2) QB_CUDA(ctx, cudaStreamWaitEvent(ctx->streams[k2], ctx->ev_fork, 0));
-    int k = 0;
-    for (int c = ctx->nclass - 1; c >= 0; --c) {   // heavy classes first
-        if (plan.nbra[c] == 0 || plan.nket[c] == 0) continue;
+    // Launch order and streams: the longest class kernels first (their measured times, once
+    // the autotuner or the class timing has run; else by class, highest angular momentum
+    // first), each on the stream with the least queued time, so that the short kernels fill
+    // the GPU while the last long ones finish.
+    int order[QB_MAX_CLASS];
+    int ncls = 0;
+    for (int c = ctx->nclass - 1; c >= 0; --c)
+        if (plan.nbra[c] > 0 && plan.nket[c] > 0) order[ncls++] = c;
+    std::stable_sort(order, order + ncls, [&](int a, int b) { return ctx->class_ms[a] > ctx->class_ms[b]; });
+    float queued[QB_NSTREAM] = {};
+    for (int k = 0; k < ncls; ++k) {
+        const int c = order[k];
         ClassWork w{ctx->d_pairs.p + plan.bra_off[c], ctx->d_pairs.p + plan.ket_off[c],
                     ctx->d_offs.p + plan.offs_off[c], plan.nbra[c], plan.same[c]};
         const int grid = ctx->nsm * std::max(1, ctx->occ[c]);
         JKArgs args{ctx->d_prims.p, ctx->d_prims32.p, ctx->boys.p, ctx->d_Dt.p, ctx->d_Jp.p, ctx->d_Kp.p, ctx->d_primcount.p + c, n, ctx->prim_eps};
-        ctx->launch[c].jk[ctx->variant[c]](w, args, grid, ctx->streams[k % QB_NSTREAM]);
-        ++k;
+        int st = k % QB_NSTREAM;
+        if (ctx->class_ms[c] > 0.f) {
+            st = 0;
+            for (int j = 1; j < QB_NSTREAM; ++j)
+                if (queued[j] < queued[st]) st = j;
+            queued[st] += ctx->class_ms[c];
+        }
+        ctx->launch[c].jk[ctx->variant[c]](w, args, grid, ctx->streams[st]);
     }
     QB_CUDA(ctx, cudaGetLastError());
     for (int j = 0; j < QB_NSTREAM; ++j) {
@@ -735,6 +751,7 @@ int qb_jk_autotune_device(qb_ctx* ctx, int repeats, int* chosen) {
         }
         ctx->variant[c] = best_v;
         ctx->occ[c] = best_occ;
+        ctx->class_ms[c] = best;
         if (chosen) chosen[c] = best_v;
     }
     QB_CUDA(ctx, cudaGetLastError());
@@ -774,6 +791,7 @@ int qb_jk_class_times_device(qb_ctx* ctx, int repeats, float* ms) {
             best = (r == 0) ? t : std::min(best, t);
         }
         ms[c] = best;
+        ctx->class_ms[c] = best;
     }
     QB_CUDA(ctx, cudaGetLastError());
     return qb_jk_device(ctx, ctx->d_D.p, ctx->d_J.p, ctx->d_K.p, ctx->schwarz, s);

@@ -135,6 +135,7 @@ struct qb_ctx {
     int nclass = 0;
     int occ[QB_MAX_CLASS] = {};
     int variant[QB_MAX_CLASS] = {};   // launcher variant per class (0 per-thread, 1 warp-cooperative)
+    float class_ms[QB_MAX_CLASS] = {};   // device time of each class kernel alone (autotuner / class timing; 0: unknown)
     float prim_eps = (float)QB_PRIM_EPS_Q;   // primitive-quartet threshold of the J/K class kernels
     int class_bra[QB_MAX_CLASS] = {}, class_ket[QB_MAX_CLASS] = {};
     long long offs_off[QB_MAX_CLASS + 1] = {};
