@@ -502,29 +502,11 @@ __global__ void __launch_bounds__(32 * WPB) qb_jk_warp_kernel(const ClassWork w,
 }
 
 // Reduce-scatter of eight values over the eight lanes of an aligned lane segment (j8 =
-// lane & 7): lane j8 ends with the segment's sum of its value j8 and adds it to row[j8].
-// Three exchange stages (lane ^ 4, ^ 2, ^ 1), each halving the values a lane holds: seven
-// FP64 adds and fourteen 32-bit shuffles per eight values, no atomics.  Every lane of the
-// warp calls it.
-__device__ __forceinline__ void qb_rs8_add(double* row, int j8, double v0, double v1, double v2, double v3,
-                                           double v4, double v5, double v6, double v7) {
-    const unsigned FULL = 0xffffffffu;
-    const bool h2 = j8 & 4, h1 = j8 & 2, h0 = j8 & 1;
-    const double a0 = (h2 ? v4 : v0) + __shfl_xor_sync(FULL, h2 ? v0 : v4, 4);
-    const double a1 = (h2 ? v5 : v1) + __shfl_xor_sync(FULL, h2 ? v1 : v5, 4);
-    const double a2 = (h2 ? v6 : v2) + __shfl_xor_sync(FULL, h2 ? v2 : v6, 4);
-    const double a3 = (h2 ? v7 : v3) + __shfl_xor_sync(FULL, h2 ? v3 : v7, 4);
-    const double b0 = (h1 ? a2 : a0) + __shfl_xor_sync(FULL, h1 ? a0 : a2, 2);
-    const double b1 = (h1 ? a3 : a1) + __shfl_xor_sync(FULL, h1 ? a1 : a3, 2);
-    const double c = (h0 ? b1 : b0) + __shfl_xor_sync(FULL, h0 ? b0 : b1, 1);
-    row[j8] += c;
-}
-
-// The same reduce-scatter through shared memory: every lane stores its eight values in its
-// own row of the warp's staging area (rows of 9 doubles, so that the reads below spread over
+// lane & 7), staged through shared memory: every lane stores its eight values in its own
+// row of the warp's staging area (rows of 9 doubles, so that the reads below spread over
 // the banks), the warp synchronises, and lane j8 sums value j8 of the eight rows of its
-// segment and adds the sum to row[j8].  Eight FP64 adds per eight values, as the shuffle
-// form, but about half its instructions.  Two staging areas alternate by batch parity, so
+// segment and adds the sum to row[j8].  Eight FP64 adds per eight values and no atomics;
+// about half the instructions of a register-shuffle exchange (three halving stages).  Two staging areas alternate by batch parity, so
 // one warp synchronisation per batch orders every store after the reads of the batch that
 // last used the area.
 __device__ __forceinline__ void qb_stage8_add(double* stage, double* row, int lane, int j8, double v0, double v1,
@@ -545,7 +527,7 @@ __device__ __forceinline__ void qb_stage8_add(double* stage, double* row, int la
 // runs them four at a time, one per 8-lane segment: in each round a segment's lanes
 // evaluate eight of its owner's primitive quartets (lanes past the owner's count run a
 // valid primitive quartet with a zero prefactor), and every group of eight VRR targets is
-// reduce-scattered over the segment (qb_rs8_add) into the owner's shared-memory row, one
+// reduce-scattered over the segment (qb_stage8_add) into the owner's shared-memory row, one
 // plain add per lane and target: no atomics, so no compare-and-swap retries when many
 // lanes serve one quartet, and no accumulator in registers or local memory.  Sorting makes
 // the four owners of a wave need similar round counts.  After a wave the whole warp runs
